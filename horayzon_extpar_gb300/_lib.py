@@ -1,0 +1,124 @@
+"""ctypes binding of libhorayzon_gb300.so (include/horayzon_gb300.h).
+
+The library is built in-tree (``horayzon_extpar_gb300/_lib/``) by
+``horayzon_extpar_gb300._build.build_library()``. Loading fails loudly when
+it is missing: there is no CPU fallback for the horizon computation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import _build
+
+_D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
+_I = C.POINTER(C.c_int32)
+
+HZ_OK, HZ_ERR_VALUE, HZ_ERR_TYPE, HZ_ERR_INDEX, HZ_ERR_CUDA, HZ_ERR_INTERNAL = range(6)
+
+#: Every symbol include/horayzon_gb300.h declares.
+EXPORTED_SYMBOLS = ("hz_default_options", "horizon_svf_comp", "hz_horizon_svf",
+                    "hz_horizon_svf_device", "hz_build_mesh", "hz_mesh_enu32",
+                    "hz_last_error", "hz_version", "hz_release_workspace")
+
+
+class Options(C.Structure):
+    _fields_ = [("size", C.c_int32), ("device", C.c_int32), ("count_work", C.c_int32),
+                ("verbose", C.c_int32), ("elev_floor_deg", C.c_double)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("num_rays", C.c_int64), ("node_visits", C.c_int64),
+                ("tri_tests", C.c_int64), ("n_tri", C.c_int32),
+                ("n_mesh_vert", C.c_int32), ("ms_h2d", C.c_double),
+                ("ms_mesh", C.c_double), ("ms_bvh", C.c_double),
+                ("ms_trace", C.c_double), ("ms_d2h", C.c_double),
+                ("ms_total", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class HorizonError(RuntimeError):
+    """A non-value failure reported by the CUDA library (status, message)."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__("horayzon_gb300 error %d: %s" % (status, message))
+        self.status = status
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path() -> str:
+    return os.environ.get("HZ_LIBRARY", _build.LIB_PATH)
+
+
+def load(build_if_missing: bool = True):
+    """The loaded CUDA library (built in-tree on first use if absent)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = library_path()
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise RuntimeError("libhorayzon_gb300.so not found at %s; build it with "
+                                   "horayzon_extpar_gb300._build.build_library()" % path)
+            path = _build.build_library()
+        L = C.CDLL(path)
+        L.hz_default_options.restype = None
+        L.hz_default_options.argtypes = [C.POINTER(Options)]
+        L.hz_last_error.restype = C.c_char_p
+        L.hz_last_error.argtypes = []
+        L.hz_version.restype = C.c_int
+        L.hz_release_workspace.restype = C.c_int
+        L.hz_release_workspace.argtypes = [C.c_int]
+        common = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                  C.c_int]
+        L.horizon_svf_comp.restype = None
+        L.horizon_svf_comp.argtypes = [_D, _D, _D, _D, _D, _I, _D, _D] + common
+        L.hz_horizon_svf.restype = C.c_int
+        L.hz_horizon_svf.argtypes = ([_D, _D, _D, _D, _D, _I, _D, _D] + common +
+                                     [C.POINTER(Options), C.POINTER(Stats)])
+        L.hz_horizon_svf_device.restype = C.c_int
+        L.hz_horizon_svf_device.argtypes = ([C.c_void_p] * 8 + common +
+                                            [C.c_void_p, C.POINTER(Options),
+                                             C.POINTER(Stats)])
+        L.hz_build_mesh.restype = C.c_int
+        L.hz_build_mesh.argtypes = [_D, _D, _D, _D, _D, _I, C.c_int, C.c_int, C.c_int,
+                                    _D, _D, _D, C.c_int, _I, C.c_int,
+                                    C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]
+        L.hz_mesh_enu32.restype = C.c_int
+        L.hz_mesh_enu32.argtypes = [_D, _D, _D, _D, _D, _I, C.c_int, C.c_int, C.c_int,
+                                    _F, C.c_int, _I, C.c_int,
+                                    C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]
+        _lib = L
+        return _lib
+
+
+def last_error() -> str:
+    return load().hz_last_error().decode("utf-8", "replace")
+
+
+def default_options(**kw) -> Options:
+    o = Options()
+    load().hz_default_options(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def check(status: int):
+    """Raise the reference's exception type for a failed call."""
+    if status == HZ_OK:
+        return
+    msg = last_error()
+    if status in (HZ_ERR_VALUE, HZ_ERR_INDEX):
+        raise ValueError(msg)
+    if status == HZ_ERR_TYPE:
+        raise TypeError(msg)
+    raise HorizonError(status, msg)

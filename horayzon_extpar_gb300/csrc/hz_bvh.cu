@@ -1,0 +1,269 @@
+// hz_bvh.cu -- linear BVH over the FP32 mesh, built on the device.
+//
+// Replaces Embree's rtcCommitScene (mo_lradtopo_horayzon.cpp:395-432):
+//   1. k_tri_bounds: triangle boxes; centre range of the boxes in x, y and
+//      the largest |coordinate| (box margin), reduced with ordered atomics;
+//   2. k_morton: 2 x 16-bit Morton keys of the box centres in the horizontal
+//      plane (the terrain is a height field, so x/y carry the locality);
+//   3. stable radix sort of (key, triangle) pairs;
+//   4. k_karras: binary radix tree (Karras, HPG 2012) with index tie-break;
+//      subtrees of <= kLeafMax triangles become leaves;
+//   5. k_gather: 48-byte triangle records in leaf order;
+//   6. k_refit: bottom-up boxes with one atomic arrival counter per node.
+// Child boxes carry a margin of 2^-20 x the largest coordinate so that box
+// culling never hides a triangle the watertight test would report. The tree
+// has the same topology as the CPU oracle's (same keys, same splits).
+#include "hz_internal.h"
+
+namespace hz {
+
+namespace {
+
+__device__ __forceinline__ uint32_t part1by1(uint32_t x) {
+  x &= 0x0000FFFFu;
+  x = (x | (x << 8)) & 0x00FF00FFu;
+  x = (x | (x << 4)) & 0x0F0F0F0Fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+
+__device__ __forceinline__ float3 load_vert(const float* __restrict__ v, int i) {
+  return make_float3(v[3LL * i], v[3LL * i + 1], v[3LL * i + 2]);
+}
+
+__global__ void k_init_bounds(unsigned* b) {
+  b[0] = 0xFFFFFFFFu;  // min cx
+  b[1] = 0xFFFFFFFFu;  // min cy
+  b[2] = 0u;           // max cx
+  b[3] = 0u;           // max cy
+  b[4] = 0u;           // max |coord|
+}
+
+__global__ void k_tri_bounds(const float* __restrict__ vert, const int* __restrict__ vot,
+                             int n, float2* __restrict__ cxy, unsigned* __restrict__ bounds) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  float cx = 0.f, cy = 0.f, m = 0.f;
+  bool valid = t < n;
+  if (valid) {
+    float3 a = load_vert(vert, vot[3LL * t]);
+    float3 b = load_vert(vert, vot[3LL * t + 1]);
+    float3 c = load_vert(vert, vot[3LL * t + 2]);
+    float lx = fminf(fminf(a.x, b.x), c.x), hx = fmaxf(fmaxf(a.x, b.x), c.x);
+    float ly = fminf(fminf(a.y, b.y), c.y), hy = fmaxf(fmaxf(a.y, b.y), c.y);
+    cx = __fmul_rn(__fadd_rn(lx, hx), 0.5f);
+    cy = __fmul_rn(__fadd_rn(ly, hy), 0.5f);
+    cxy[t] = make_float2(cx, cy);
+    m = fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(b.x))),
+              fmaxf(fmaxf(fabsf(b.y), fabsf(b.z)),
+                    fmaxf(fmaxf(fabsf(c.x), fabsf(c.y)), fabsf(c.z))));
+  }
+  // Warp-level reduction, then one atomic per warp.
+  unsigned mnx = valid ? f2ord(cx) : 0xFFFFFFFFu, mny = valid ? f2ord(cy) : 0xFFFFFFFFu;
+  unsigned mxx = valid ? f2ord(cx) : 0u, mxy = valid ? f2ord(cy) : 0u;
+  unsigned mm = valid ? f2ord(m) : 0u;
+  mnx = __reduce_min_sync(0xffffffffu, mnx);
+  mny = __reduce_min_sync(0xffffffffu, mny);
+  mxx = __reduce_max_sync(0xffffffffu, mxx);
+  mxy = __reduce_max_sync(0xffffffffu, mxy);
+  mm = __reduce_max_sync(0xffffffffu, mm);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&bounds[0], mnx);
+    atomicMin(&bounds[1], mny);
+    atomicMax(&bounds[2], mxx);
+    atomicMax(&bounds[3], mxy);
+    atomicMax(&bounds[4], mm);
+  }
+}
+
+__global__ void k_morton(const float2* __restrict__ cxy, int n,
+                         const unsigned* __restrict__ bounds, uint32_t* __restrict__ keys,
+                         int32_t* __restrict__ vals) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const float mnx = ord2f(bounds[0]), mny = ord2f(bounds[1]);
+  const float mxx = ord2f(bounds[2]), mxy = ord2f(bounds[3]);
+  const float ex = __fsub_rn(mxx, mnx), ey = __fsub_rn(mxy, mny);
+  const float sx = ex > 0.f ? __fdiv_rn(65535.0f, ex) : 0.f;
+  const float sy = ey > 0.f ? __fdiv_rn(65535.0f, ey) : 0.f;
+  const float2 c = cxy[t];
+  const float fx = __fmul_rn(__fsub_rn(c.x, mnx), sx);
+  const float fy = __fmul_rn(__fsub_rn(c.y, mny), sy);
+  const uint32_t qx = fx <= 0.f ? 0u : (fx >= 65535.0f ? 65535u : (uint32_t)fx);
+  const uint32_t qy = fy <= 0.f ? 0u : (fy >= 65535.0f ? 65535u : (uint32_t)fy);
+  keys[t] = part1by1(qx) | (part1by1(qy) << 1);
+  vals[t] = t;
+}
+
+__device__ __forceinline__ int delta(const uint32_t* __restrict__ keys, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  const uint32_t a = keys[i], b = keys[j];
+  if (a != b) return __clz(a ^ b);
+  return 32 + __clz((uint32_t)(i ^ j));
+}
+
+__global__ void k_karras(const uint32_t* __restrict__ keys, int n, Node* __restrict__ nodes,
+                         int* __restrict__ parent, int* __restrict__ nsize,
+                         int* __restrict__ counter) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = delta(keys, n, i, i - d);
+  int lmax = 2;
+  while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t >= 1; t >>= 1)
+    if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = i + l * d;
+  const int dnode = delta(keys, n, i, j);
+  int s = 0, t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+  } while (t > 1);
+  const int gamma = i + s * d + (d < 0 ? d : 0);
+  const int first = min(i, j), last = max(i, j);
+  const int nl = gamma - first + 1, nr = last - gamma;
+  const int c0 = nl <= kLeafMax ? leaf_ref(first, nl) : gamma;
+  const int c1 = nr <= kLeafMax ? leaf_ref(gamma + 1, nr) : gamma + 1;
+  nsize[i] = last - first + 1;
+  counter[i] = 0;
+  nodes[i].d = make_float4(__int_as_float(c0), __int_as_float(c1), 0.f, 0.f);
+  if (last - first + 1 > kLeafMax) {  // live node: its internal children are live
+    if (c0 >= 0) parent[c0] = (i << 1) | 0;
+    if (c1 >= 0) parent[c1] = (i << 1) | 1;
+  }
+}
+
+__global__ void k_gather(const float* __restrict__ vert, const int* __restrict__ vot,
+                         const int32_t* __restrict__ order, int n, Tri* __restrict__ tris) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int t = order[s];
+  const float3 a = load_vert(vert, vot[3LL * t]);
+  const float3 b = load_vert(vert, vot[3LL * t + 1]);
+  const float3 c = load_vert(vert, vot[3LL * t + 2]);
+  Tri r;
+  r.v0 = make_float4(a.x, a.y, a.z, __int_as_float(t));
+  r.v1 = make_float4(b.x, b.y, b.z, 0.f);
+  r.v2 = make_float4(c.x, c.y, c.z, 0.f);
+  tris[s] = r;
+}
+
+struct Box {
+  float lx, ly, lz, hx, hy, hz;
+};
+
+__device__ __forceinline__ Box leaf_box(const Tri* __restrict__ tris, int ref, float pad) {
+  const int s = leaf_start(ref), c = leaf_count(ref);
+  Box b = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  for (int k = s; k < s + c; k++) {
+    const Tri t = tris[k];
+    const float4 v[3] = {t.v0, t.v1, t.v2};
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      b.lx = fminf(b.lx, v[q].x); b.hx = fmaxf(b.hx, v[q].x);
+      b.ly = fminf(b.ly, v[q].y); b.hy = fmaxf(b.hy, v[q].y);
+      b.lz = fminf(b.lz, v[q].z); b.hz = fmaxf(b.hz, v[q].z);
+    }
+  }
+  b.lx = __fsub_rn(b.lx, pad); b.ly = __fsub_rn(b.ly, pad); b.lz = __fsub_rn(b.lz, pad);
+  b.hx = __fadd_rn(b.hx, pad); b.hy = __fadd_rn(b.hy, pad); b.hz = __fadd_rn(b.hz, pad);
+  return b;
+}
+
+__device__ __forceinline__ void store_child_box(Node* node, int side, const Box& b) {
+  float* base = reinterpret_cast<float*>(node);
+  // a / b: (lo.x, hi.x, lo.y, hi.y) of child 0 / 1; c: (lo.z, hi.z) per child.
+  __stcg(reinterpret_cast<float4*>(base + 4 * side), make_float4(b.lx, b.hx, b.ly, b.hy));
+  __stcg(reinterpret_cast<float2*>(base + 8 + 2 * side), make_float2(b.lz, b.hz));
+}
+
+__device__ __forceinline__ Box union_of_children(const Node* node) {
+  const float* base = reinterpret_cast<const float*>(node);
+  const float4 a = __ldcg(reinterpret_cast<const float4*>(base));
+  const float4 b = __ldcg(reinterpret_cast<const float4*>(base + 4));
+  const float4 c = __ldcg(reinterpret_cast<const float4*>(base + 8));
+  Box u;
+  u.lx = fminf(a.x, b.x); u.hx = fmaxf(a.y, b.y);
+  u.ly = fminf(a.z, b.z); u.hy = fmaxf(a.w, b.w);
+  u.lz = fminf(c.x, c.z); u.hz = fmaxf(c.y, c.w);
+  return u;
+}
+
+__global__ void k_refit(Node* __restrict__ nodes, const Tri* __restrict__ tris, int n,
+                        const int* __restrict__ parent, const int* __restrict__ nsize,
+                        int* __restrict__ counter, const unsigned* __restrict__ bounds) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1 || nsize[i] <= kLeafMax) return;
+  const float pad = __fmul_rn(ord2f(bounds[4]), 9.5367431640625e-07f);
+  const float4 d = nodes[i].d;
+  const int c0 = __float_as_int(d.x), c1 = __float_as_int(d.y);
+  int arrivals = 0;
+  if (c0 < 0) { store_child_box(&nodes[i], 0, leaf_box(tris, c0, pad)); arrivals++; }
+  if (c1 < 0) { store_child_box(&nodes[i], 1, leaf_box(tris, c1, pad)); arrivals++; }
+  if (arrivals == 0) return;
+  __threadfence();
+  int old = atomicAdd(&counter[i], arrivals);
+  if (old + arrivals != 2) return;
+  int node = i;
+  while (node != 0) {
+    __threadfence();
+    const Box u = union_of_children(&nodes[node]);
+    const int p = parent[node];
+    store_child_box(&nodes[p >> 1], p & 1, u);
+    __threadfence();
+    old = atomicAdd(&counter[p >> 1], 1);
+    if (old + 1 != 2) return;
+    node = p >> 1;
+  }
+}
+
+// n_tri <= kLeafMax: one node, child 0 = leaf of all triangles, child 1 empty.
+__global__ void k_small_root(Node* nodes, const Tri* __restrict__ tris, int n,
+                             const unsigned* __restrict__ bounds) {
+  const float pad = __fmul_rn(ord2f(bounds[4]), 9.5367431640625e-07f);
+  const Box b = leaf_box(tris, leaf_ref(0, n), pad);
+  Node r;
+  r.a = make_float4(b.lx, b.hx, b.ly, b.hy);
+  r.b = make_float4(INFINITY, -INFINITY, INFINITY, -INFINITY);
+  r.c = make_float4(b.lz, b.hz, INFINITY, -INFINITY);
+  r.d = make_float4(__int_as_float(leaf_ref(0, n)), __int_as_float(kEmptyRef), 0.f, 0.f);
+  nodes[0] = r;
+}
+
+}  // namespace
+
+size_t bvh_scratch_bytes(long long n) {
+  if (n < 1) n = 1;
+  size_t b = 0;
+  b += 4 * sizeof(uint32_t) * (size_t)n;  // keys, vals, keys_alt, vals_alt
+  b += sizeof(float2) * (size_t)n;
+  b += 3 * sizeof(int) * (size_t)n;       // parent, nsize, counter
+  b += 64;                                // bounds
+  b += radix_scratch_u32(n);
+  return b + 8 * 256;                     // alignment slack
+}
+
+cudaError_t bvh_build(const float* vert32, const int* vot, int n, Node* nodes, Tri* tris,
+                      const BvhScratch& sc, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_init_bounds<<<1, 1, 0, s>>>(sc.bounds);
+  k_tri_bounds<<<grid_for(n, 256), 256, 0, s>>>(vert32, vot, n, sc.cxy, sc.bounds);
+  k_morton<<<grid_for(n, 256), 256, 0, s>>>(sc.cxy, n, sc.bounds, sc.keys, sc.vals);
+  cudaError_t e = radix_sort_pairs(sc.keys, sc.vals, sc.keys_alt, sc.vals_alt, n, 32,
+                                   sc.sort_scratch, s);
+  if (e != cudaSuccess) return e;
+  k_gather<<<grid_for(n, 256), 256, 0, s>>>(vert32, vot, sc.vals, n, tris);
+  if (n <= kLeafMax) {
+    k_small_root<<<1, 1, 0, s>>>(nodes, tris, n, sc.bounds);
+    return cudaGetLastError();
+  }
+  k_karras<<<grid_for(n - 1, 256), 256, 0, s>>>(sc.keys, n, nodes, sc.parent, sc.nsize,
+                                                sc.counter);
+  k_refit<<<grid_for(n - 1, 256), 256, 0, s>>>(nodes, tris, n, sc.parent, sc.nsize,
+                                               sc.counter, sc.bounds);
+  return cudaGetLastError();
+}
+
+}  // namespace hz

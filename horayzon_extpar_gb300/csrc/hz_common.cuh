@@ -1,0 +1,86 @@
+// hz_common.cuh -- shared device types, constants and helpers of the
+// horizon / sky-view-factor library.
+//
+// Every translation unit of the library is compiled with -fmad=false: the
+// reference's FP64 geometry (mo_lradtopo_horayzon.cpp:78-201, 490-555,
+// 694-754) and the FP32 triangle test are evaluated with one rounding per
+// operation, exactly as the host code does, so that hit decisions and the
+// lattice of tested elevation angles are reproduced bit for bit. Multiply-adds
+// that do not need to match are written explicitly with __fmaf_rn.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hz {
+
+constexpr double kEarthRadius = 6371229.0;  // mo_lradtopo_horayzon.cpp:584
+constexpr double kPi = 3.14159265358979323846;
+constexpr int kLeafMax = 4;                 // triangles per BVH leaf
+constexpr int kStackDepth = 64;             // >= LBVH depth (32 key + 32 index bits)
+constexpr int kEmptyRef = INT32_MIN;        // no child / empty tree
+constexpr int kMaxUpSteps = 720;            // one full turn of 0.5 deg steps
+
+// Error bits raised by kernels (device word, read back by the host).
+enum : int {
+  kErrBadIndex = 1,     // cells_of_vertex entry outside [0, ncell) and != -2
+  kErrStack = 2,        // traversal stack overflow
+  kErrMeshCapacity = 4  // mesh emission beyond the sized buffers
+};
+
+// Leaf references are negative: ~(start << 3 | (count - 1)).
+__host__ __device__ __forceinline__ int leaf_ref(int start, int count) {
+  return ~((start << 3) | (count - 1));
+}
+__host__ __device__ __forceinline__ int leaf_start(int ref) { return (~ref) >> 3; }
+__host__ __device__ __forceinline__ int leaf_count(int ref) { return ((~ref) & 7) + 1; }
+
+// BVH2 node, 64 bytes: both child boxes and both child references.
+//   a = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   b = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   c = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   d = (child0, child1, -, -) as int bits
+struct __align__(16) Node {
+  float4 a, b, c, d;
+};
+
+// Triangle record, 48 bytes: v0.xyz + original id, v1.xyz, v2.xyz.
+struct __align__(16) Tri {
+  float4 v0, v1, v2;
+};
+
+// Global ENU frame of the domain (mo_lradtopo_horayzon.cpp:611-644).
+struct Frame {
+  double sin_lon, cos_lon, sin_lat, cos_lat;
+  double xe, ye, ze;          // ECEF of the ENU origin on the sphere
+  double cyx, cyy, czx, czy;  // (-sin_lat)*cos_lon, sin_lat*sin_lon,
+                              // cos_lat*cos_lon, cos_lat*sin_lon
+  double3 centre;             // Earth centre in ENU
+  double3 pole;               // North Pole in ENU
+};
+
+// Order-preserving float <-> uint mapping for atomicMin/atomicMax.
+__device__ __forceinline__ unsigned f2ord(float f) {
+  unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+__host__ __forceinline__ float ord2f_host(unsigned u) {
+  unsigned v = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+  float f;
+  __builtin_memcpy(&f, &v, 4);
+  return f;
+}
+
+// ---------------------------------------------------------------------------
+// Launch helpers (host side, defined in hz_kernels_*.cu)
+// ---------------------------------------------------------------------------
+
+inline unsigned grid_for(long long n, int block) {
+  long long g = (n + block - 1) / block;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+}  // namespace hz

@@ -1,0 +1,90 @@
+// hz_internal.h -- launch functions shared between the library's translation
+// units (mesh, sort, BVH, trace, API). Every function enqueues work on the
+// given stream and returns the launch status; nothing here synchronises.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hz_common.cuh"
+
+namespace hz {
+
+// ---- hz_scan_sort.cu -------------------------------------------------------
+// Exclusive prefix sum of n values; total to *d_total (device). `partials`
+// needs scan_partials(n) elements.
+long long scan_partials(long long n);
+cudaError_t scan_exclusive_u64(const unsigned long long* in, unsigned long long* out,
+                               long long n, unsigned long long* d_total,
+                               unsigned long long* partials, cudaStream_t s);
+cudaError_t scan_exclusive_u32(const uint32_t* in, uint32_t* out, long long n,
+                               uint32_t* d_total, uint32_t* partials, cudaStream_t s);
+// Stable LSD radix sort of (key, value) pairs on the low `bits` key bits.
+// Scratch sizes from radix_scratch_u32(n). Result ends in (keys, vals).
+size_t radix_scratch_u32(long long n);
+cudaError_t radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_alt,
+                             int32_t* vals_alt, long long n, int bits, void* scratch,
+                             cudaStream_t s);
+
+// ---- hz_mesh.cu -------------------------------------------------------------
+// mo_lradtopo_horayzon.cpp:228-317: per ICON vertex, the triangle count in the
+// low 32 bits and the appended-vertex count (grid_type 1) in the high 32 bits.
+cudaError_t mesh_count(const int* cov, int nv, int ncell, int grid_type,
+                       unsigned long long* packed, int* err, cudaStream_t s);
+// Emission at the scanned offsets. Appended vertices go to add_{lon,lat,h}.
+cudaError_t mesh_emit(const double* clon, const double* clat, const double* hsurf,
+                      const double* vlon, const double* vlat, const int* cov, int nv,
+                      int ncell, int grid_type, const unsigned long long* offsets,
+                      int* vot, double* add_lon, double* add_lat, double* add_h,
+                      cudaStream_t s);
+// cpp:158-169 for all mesh vertices (cells first, then appended vertices) and
+// per-block partial sums of the cell ECEF coordinates (cpp:624-631).
+int ecef_blocks(int ncell);
+cudaError_t mesh_ecef(const double* clon, const double* clat, const double* hsurf,
+                      const double* add_lon, const double* add_lat, const double* add_h,
+                      int ncell, int nadd, double* ecef, double* block_sums,
+                      double* d_origin_sum, cudaStream_t s);
+// cpp:178-201: FP32 ENU of every mesh vertex, FP64 ENU of every cell.
+cudaError_t mesh_enu(const double* ecef, int nmv, int ncell, const Frame& f,
+                     float* vert32, double* cell_enu, cudaStream_t s);
+
+// ---- hz_bvh.cu --------------------------------------------------------------
+struct BvhScratch {
+  uint32_t* keys;       // n
+  int32_t* vals;        // n
+  uint32_t* keys_alt;   // n
+  int32_t* vals_alt;    // n
+  float2* cxy;          // n triangle-box centres (x, y)
+  int* parent;          // n (node -> parent << 1 | side)
+  int* nsize;           // n (range size per internal node)
+  int* counter;         // n (refit arrivals)
+  unsigned* bounds;     // 5: min cx, min cy, max cx, max cy, max |coord| (ordered)
+  void* sort_scratch;   // radix_scratch_u32(n)
+};
+size_t bvh_scratch_bytes(long long n_tri);
+// Builds nodes[n_tri - 1] (or one node when n_tri <= kLeafMax) and tris[n_tri];
+// the root is node 0. n_tri == 0 leaves the tree empty.
+cudaError_t bvh_build(const float* vert32, const int* vot, int n_tri, Node* nodes,
+                      Tri* tris, const BvhScratch& sc, cudaStream_t s);
+
+// ---- hz_trace.cu ------------------------------------------------------------
+struct TraceParams {
+  const double* cell_enu;   // [3 * ncell] FP64 ENU of cell centres
+  int ncell;
+  const Node* nodes;
+  const Tri* tris;
+  int root;                 // 0, or kEmptyRef for an empty mesh
+  double3 centre, pole;     // Earth centre / North Pole in ENU
+  double ray_org_elev;
+  float tfar;               // (float)dist_search, cpp:587
+  int nhori, refine, L, svf_type;
+  double hori_acc, elev_floor;
+  double azim_sin, azim_cos, elev_sin_2ha, elev_cos_2ha, shift_sin, shift_cos;
+  double* horizon;          // [nhori * ncell] degrees
+  double* skyview;          // [ncell]
+  unsigned long long* counters;  // [0] rays, [1] node visits, [2] triangle tests
+  int* err;
+};
+cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s);
+
+}  // namespace hz

@@ -1,0 +1,251 @@
+// hz_mesh.cu -- triangle-mesh assembly from the ICON grid and the geodetic
+// frame transforms, one thread per ICON vertex / mesh vertex.
+//
+// mesh_count + scan + mesh_emit restate build_triangle_mesh
+// (mo_lradtopo_horayzon.cpp:228-317) as a data-parallel pass: each vertex
+// counts its triangles (and, for grid_type 1, its appended vertex), an
+// exclusive scan turns the counts into output offsets, and each vertex then
+// writes its triangles at its offset. The output order is the reference's:
+// triangles by ICON vertex, appended vertices numbered ncell + k in vertex
+// order. Neighbour cells are ordered by atan2(dlon, dlat) wrapped to [0, 2pi)
+// with a stable insertion sort (std::sort of <= 16 elements, cpp:137-146, is
+// an insertion sort). Sorted positions are mapped back to their
+// cells_of_vertex slots; the reference indexes rows by position among the
+// valid entries (cpp:265-271), which is the same whenever -2 entries trail.
+#include "hz_internal.h"
+
+namespace hz {
+
+namespace {
+
+__global__ void k_mesh_count(const int* __restrict__ cov, int nv, int ncell,
+                             int grid_type, unsigned long long* __restrict__ packed,
+                             int* __restrict__ err) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  int n = 0;
+  bool bad = false;
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    int c = cov[(long long)nv * j + v];
+    if (c != -2) {
+      if (c < 0 || c >= ncell) bad = true;
+      else n++;
+    }
+  }
+  if (bad) atomicOr(err, kErrBadIndex);
+  unsigned tri, add;
+  if (grid_type == 0) {
+    tri = n >= 3 ? (unsigned)(n - 2) : 0u;
+    add = 0u;
+  } else {
+    tri = n == 6 ? 6u : 0u;
+    add = n == 6 ? 1u : 0u;
+  }
+  packed[v] = ((unsigned long long)add << 32) | tri;
+}
+
+__global__ void k_mesh_emit(const double* __restrict__ clon, const double* __restrict__ clat,
+                            const double* __restrict__ hsurf, const double* __restrict__ vlon,
+                            const double* __restrict__ vlat, const int* __restrict__ cov,
+                            int nv, int ncell, int grid_type,
+                            const unsigned long long* __restrict__ offsets,
+                            int* __restrict__ vot, double* __restrict__ add_lon,
+                            double* __restrict__ add_lat, double* __restrict__ add_h) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  double ang[6];
+  int cell[6];
+  int n = 0;
+  double hsum = 0.0;
+  const double lon_v = vlon[v], lat_v = vlat[v];
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    int c = cov[(long long)nv * j + v];
+    if (c != -2 && c >= 0 && c < ncell) {
+      double a = atan2(clon[c] - lon_v, clat[c] - lat_v);
+      if (a < 0.0) a += 2.0 * kPi;
+      ang[n] = a;
+      cell[n] = c;
+      n++;
+      hsum += hsurf[c];
+    }
+  }
+  // Stable insertion sort of (angle, cell) pairs by angle.
+  for (int k = 1; k < n; k++) {
+    double a = ang[k];
+    int c = cell[k];
+    int m = k - 1;
+    while (m >= 0 && a < ang[m]) {
+      ang[m + 1] = ang[m];
+      cell[m + 1] = cell[m];
+      m--;
+    }
+    ang[m + 1] = a;
+    cell[m + 1] = c;
+  }
+  const unsigned long long off = offsets[v];
+  long long t = (long long)(off & 0xFFFFFFFFull);
+  if (grid_type == 0) {
+    if (n >= 3) {
+      for (int k = 0; k < n - 2; k++, t++) {
+        vot[3 * t + 0] = cell[0];
+        vot[3 * t + 1] = cell[k + 1];
+        vot[3 * t + 2] = cell[k + 2];
+      }
+    }
+  } else if (n == 6) {
+    int add = (int)(off >> 32);
+    add_lon[add] = lon_v;
+    add_lat[add] = lat_v;
+    add_h[add] = hsum / 6.0;
+    const int id = ncell + add;
+#pragma unroll
+    for (int k = 0; k < 6; k++, t++) {
+      vot[3 * t + 0] = cell[k];
+      vot[3 * t + 1] = cell[k == 5 ? 0 : k + 1];
+      vot[3 * t + 2] = id;
+    }
+  }
+}
+
+constexpr int kEcefThreads = 256;
+
+__global__ void k_mesh_ecef(const double* __restrict__ clon, const double* __restrict__ clat,
+                            const double* __restrict__ hsurf,
+                            const double* __restrict__ add_lon,
+                            const double* __restrict__ add_lat,
+                            const double* __restrict__ add_h, int ncell, int nadd,
+                            double* __restrict__ ecef, double* __restrict__ block_sums) {
+  __shared__ double sx[kEcefThreads], sy[kEcefThreads], sz[kEcefThreads];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nmv = ncell + nadd;
+  double x = 0.0, y = 0.0, z = 0.0;
+  if (i < nmv) {
+    double lon, lat, h;
+    if (i < ncell) {
+      lon = clon[i]; lat = clat[i]; h = hsurf[i];
+    } else {
+      lon = add_lon[i - ncell]; lat = add_lat[i - ncell]; h = add_h[i - ncell];
+    }
+    const double sin_lon = sin(lon), cos_lon = cos(lon);
+    const double sin_lat = sin(lat), cos_lat = cos(lat);
+    x = (kEarthRadius + h) * cos_lat * cos_lon;
+    y = (kEarthRadius + h) * cos_lat * sin_lon;
+    z = (kEarthRadius + h) * sin_lat;
+    ecef[3LL * i + 0] = x;
+    ecef[3LL * i + 1] = y;
+    ecef[3LL * i + 2] = z;
+  }
+  // Partial sums over cells only (fixed tree order: deterministic).
+  const bool is_cell = i < ncell;
+  sx[threadIdx.x] = is_cell ? x : 0.0;
+  sy[threadIdx.x] = is_cell ? y : 0.0;
+  sz[threadIdx.x] = is_cell ? z : 0.0;
+  __syncthreads();
+  for (int o = kEcefThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sx[threadIdx.x] += sx[threadIdx.x + o];
+      sy[threadIdx.x] += sy[threadIdx.x + o];
+      sz[threadIdx.x] += sz[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    block_sums[3LL * blockIdx.x + 0] = sx[0];
+    block_sums[3LL * blockIdx.x + 1] = sy[0];
+    block_sums[3LL * blockIdx.x + 2] = sz[0];
+  }
+}
+
+__global__ void k_sum_blocks(const double* __restrict__ block_sums, int nb,
+                             double* __restrict__ out) {
+  __shared__ double sx[1024], sy[1024], sz[1024];
+  double x = 0.0, y = 0.0, z = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    x += block_sums[3LL * b + 0];
+    y += block_sums[3LL * b + 1];
+    z += block_sums[3LL * b + 2];
+  }
+  sx[threadIdx.x] = x;
+  sy[threadIdx.x] = y;
+  sz[threadIdx.x] = z;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sx[threadIdx.x] += sx[threadIdx.x + o];
+      sy[threadIdx.x] += sy[threadIdx.x + o];
+      sz[threadIdx.x] += sz[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = sx[0];
+    out[1] = sy[0];
+    out[2] = sz[0];
+  }
+}
+
+__global__ void k_mesh_enu(const double* __restrict__ ecef, int nmv, int ncell, Frame f,
+                           float* __restrict__ vert32, double* __restrict__ cell_enu) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nmv) return;
+  const double dx = ecef[3LL * i + 0] - f.xe;
+  const double dy = ecef[3LL * i + 1] - f.ye;
+  const double dz = ecef[3LL * i + 2] - f.ze;
+  // mo_lradtopo_horayzon.cpp:189-196, operation for operation.
+  const double xn = (-f.sin_lon) * dx + f.cos_lon * dy;
+  const double yn = f.cyx * dx - f.cyy * dy + f.cos_lat * dz;
+  const double zn = f.czx * dx + f.czy * dy + f.sin_lat * dz;
+  vert32[3LL * i + 0] = (float)xn;
+  vert32[3LL * i + 1] = (float)yn;
+  vert32[3LL * i + 2] = (float)zn;
+  if (i < ncell) {
+    cell_enu[3LL * i + 0] = xn;
+    cell_enu[3LL * i + 1] = yn;
+    cell_enu[3LL * i + 2] = zn;
+  }
+}
+
+}  // namespace
+
+cudaError_t mesh_count(const int* cov, int nv, int ncell, int grid_type,
+                       unsigned long long* packed, int* err, cudaStream_t s) {
+  if (nv <= 0) return cudaSuccess;
+  k_mesh_count<<<grid_for(nv, 256), 256, 0, s>>>(cov, nv, ncell, grid_type, packed, err);
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_emit(const double* clon, const double* clat, const double* hsurf,
+                      const double* vlon, const double* vlat, const int* cov, int nv,
+                      int ncell, int grid_type, const unsigned long long* offsets,
+                      int* vot, double* add_lon, double* add_lat, double* add_h,
+                      cudaStream_t s) {
+  if (nv <= 0) return cudaSuccess;
+  k_mesh_emit<<<grid_for(nv, 128), 128, 0, s>>>(clon, clat, hsurf, vlon, vlat, cov, nv,
+                                                ncell, grid_type, offsets, vot, add_lon,
+                                                add_lat, add_h);
+  return cudaGetLastError();
+}
+
+int ecef_blocks(int ncell_plus_nadd) { return (int)grid_for(ncell_plus_nadd, kEcefThreads); }
+
+cudaError_t mesh_ecef(const double* clon, const double* clat, const double* hsurf,
+                      const double* add_lon, const double* add_lat, const double* add_h,
+                      int ncell, int nadd, double* ecef, double* block_sums,
+                      double* d_origin_sum, cudaStream_t s) {
+  int nb = ecef_blocks(ncell + nadd);
+  k_mesh_ecef<<<nb, kEcefThreads, 0, s>>>(clon, clat, hsurf, add_lon, add_lat, add_h, ncell,
+                                          nadd, ecef, block_sums);
+  k_sum_blocks<<<1, 1024, 0, s>>>(block_sums, nb, d_origin_sum);
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_enu(const double* ecef, int nmv, int ncell, const Frame& f, float* vert32,
+                     double* cell_enu, cudaStream_t s) {
+  if (nmv <= 0) return cudaSuccess;
+  k_mesh_enu<<<grid_for(nmv, 256), 256, 0, s>>>(ecef, nmv, ncell, f, vert32, cell_enu);
+  return cudaGetLastError();
+}
+
+}  // namespace hz

@@ -1,0 +1,154 @@
+/*
+ * horayzon_gb300.h -- C ABI of the GB300 (sm_103a) terrain-horizon and
+ * sky-view-factor library (libhorayzon_gb300.so).
+ *
+ * The library replaces the reference's horizon_svf_comp
+ * (mo_lradtopo_horayzon.h:4-11, mo_lradtopo_horayzon.cpp:562-785) and the
+ * Cython binding above it (horizon_svf.pyx:15-124). Inputs and outputs keep
+ * the reference layouts:
+ *
+ *   clon, clat, hsurf   [num_cell]        FP64 cell circumcentres [rad], elevation [m]
+ *   vlon, vlat          [num_vertex]      FP64 ICON vertices [rad]
+ *   cells_of_vertex     [6][num_vertex]   int32, C order, -2 = no cell
+ *   horizon             [num_hori][num_cell]  FP64 horizon angle [deg]
+ *   skyview             [num_cell]        FP64 sky view factor [-]
+ *
+ * Every entry point except horizon_svf_comp returns a status (HZ_OK = 0) and
+ * leaves a message for hz_last_error(). No entry point aborts the process.
+ * Calls on one device are serialised by the library; the caller owns all
+ * buffers. Internally each call builds the triangle mesh, the LBVH and runs
+ * the horizon search on one GPU.
+ */
+#ifndef HORAYZON_GB300_H
+#define HORAYZON_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HZ_VERSION 100  /* 1.0.0 */
+
+enum {
+    HZ_OK = 0,
+    HZ_ERR_VALUE = 1,     /* argument out of range (horizon_svf.pyx:79-103, ValueError) */
+    HZ_ERR_TYPE = 2,      /* ray_org_elev < 0.1 (horizon_svf.pyx:98-99, TypeError) */
+    HZ_ERR_INDEX = 3,     /* cells_of_vertex entry outside [0, num_cell) and != -2
+                             (horizon_svf.pyx:88-90) */
+    HZ_ERR_CUDA = 4,      /* CUDA runtime error (no device, out of memory, ...) */
+    HZ_ERR_INTERNAL = 5   /* traversal-stack overflow or mesh capacity exceeded */
+};
+
+typedef struct hz_options {
+    int32_t size;            /* sizeof(hz_options); filled by hz_default_options */
+    int32_t device;          /* CUDA device ordinal; -1 = the calling thread's current device */
+    int32_t count_work;      /* 1: also count BVH node visits and triangle tests */
+    int32_t verbose;         /* 1: print the reference's progress lines to stdout */
+    double elev_floor_deg;   /* lower bound of the downward elevation walk; the
+                                reference's is -85 (mo_lradtopo_horayzon.cpp:578) */
+} hz_options;
+
+typedef struct hz_stats {
+    int64_t num_rays;        /* rays cast (reference prints it, cpp:769) */
+    int64_t node_visits;     /* with count_work: BVH internal-node visits */
+    int64_t tri_tests;       /* with count_work: ray/triangle tests */
+    int32_t n_tri;           /* triangles in the mesh (cpp:314-315) */
+    int32_t n_mesh_vert;     /* mesh vertices: cells + appended ICON vertices */
+    double ms_h2d;           /* host->device copies (host entry points) */
+    double ms_mesh;          /* mesh assembly + geodetic frames */
+    double ms_bvh;           /* LBVH build */
+    double ms_trace;         /* horizon search + SVF */
+    double ms_d2h;           /* device->host copies (host entry points) */
+    double ms_total;         /* whole call, wall clock */
+} hz_stats;
+
+/* Fills *opt with the defaults (device -1, elev_floor_deg -85, counters off). */
+void hz_default_options(hz_options* opt);
+
+/*
+ * Drop-in for the reference function of the same name and signature
+ * (mo_lradtopo_horayzon.h:4-11, mo_lradtopo_horayzon.cpp:562-569), with C
+ * linkage so that Fortran (ISO_C_BINDING) and ctypes can bind it, as the
+ * commented extern "C" at mo_lradtopo_horayzon.cpp:561 intends. Host buffers.
+ * Like the reference it returns nothing; on an error it prints
+ * hz_last_error() to stderr and fills horizon and skyview with NaN.
+ */
+void horizon_svf_comp(double* clon, double* clat, double* hsurf,
+                      double* vlon, double* vlat,
+                      int* cells_of_vertex,
+                      double* horizon, double* skyview,
+                      int num_cell, int num_vertex, int num_hori,
+                      int grid_type, double dist_search,
+                      double ray_org_elev, int refine_factor,
+                      int svf_type);
+
+/*
+ * Same computation with a status, options and statistics. Host buffers; the
+ * arguments are validated as horizon_svf.pyx:79-103 does. opt and stats may
+ * be NULL.
+ */
+int hz_horizon_svf(const double* clon, const double* clat, const double* hsurf,
+                   const double* vlon, const double* vlat,
+                   const int32_t* cells_of_vertex,
+                   double* horizon, double* skyview,
+                   int num_cell, int num_vertex, int num_hori,
+                   int grid_type, double dist_search,
+                   double ray_org_elev, int refine_factor, int svf_type,
+                   const hz_options* opt, hz_stats* stats);
+
+/*
+ * Same as hz_horizon_svf with every array already in device memory of the
+ * selected device. Work is enqueued on `stream` (a cudaStream_t; NULL = the
+ * legacy default stream) and the call returns when it has completed. No
+ * reference counterpart: it lets callers that keep fields on the GPU skip the
+ * host round trip of horizon_svf.pyx:106-122.
+ */
+int hz_horizon_svf_device(const double* clon, const double* clat, const double* hsurf,
+                          const double* vlon, const double* vlat,
+                          const int32_t* cells_of_vertex,
+                          double* horizon, double* skyview,
+                          int num_cell, int num_vertex, int num_hori,
+                          int grid_type, double dist_search,
+                          double ray_org_elev, int refine_factor, int svf_type,
+                          void* stream, const hz_options* opt, hz_stats* stats);
+
+/*
+ * Triangle-mesh assembly alone (mo_lradtopo_horayzon.cpp:228-317), on the
+ * GPU, host buffers: mesh vertex (lon, lat, elevation) for the cells followed
+ * by the appended ICON vertices, and three vertex indices per triangle.
+ * Capacities: cap_vert >= num_cell + num_vertex, cap_tri >= 6 * num_vertex.
+ */
+int hz_build_mesh(const double* clon, const double* clat, const double* hsurf,
+                  const double* vlon, const double* vlat,
+                  const int32_t* cells_of_vertex, int num_cell, int num_vertex,
+                  int grid_type, double* mesh_lon, double* mesh_lat, double* mesh_h,
+                  int cap_vert, int32_t* vertex_of_triangle, int cap_tri,
+                  int* n_mesh_vert, int* n_tri, int device);
+
+/*
+ * The FP32 vertices in the domain's ENU frame that rays are intersected with
+ * (mo_lradtopo_horayzon.cpp:611-644, 403-410), plus the triangle list.
+ * Capacities as for hz_build_mesh; enu32 holds 3 * cap_vert floats.
+ */
+int hz_mesh_enu32(const double* clon, const double* clat, const double* hsurf,
+                  const double* vlon, const double* vlat,
+                  const int32_t* cells_of_vertex, int num_cell, int num_vertex,
+                  int grid_type, float* enu32, int cap_vert,
+                  int32_t* vertex_of_triangle, int cap_tri,
+                  int* n_mesh_vert, int* n_tri, int device);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* hz_last_error(void);
+
+/* HZ_VERSION of the loaded library. */
+int hz_version(void);
+
+/* Frees the cached device workspace of `device` (-1 = all devices). */
+int hz_release_workspace(int device);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HORAYZON_GB300_H */

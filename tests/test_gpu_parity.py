@@ -1,0 +1,188 @@
+"""GPU path (through the C ABI) against the reference's golden outputs and
+the CPU oracle. Bar: identical horizons on >= 99.9 % of (cell, azimuth) and
+|dSVF| <= 1e-3; in practice the hit decisions are bit-identical, so the
+tests also require exact agreement of horizons (1e-9 deg) on >= 99.9 %."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+from horayzon_extpar_gb300 import _lib, build_mesh, horizon_svf_comp_py, mesh_enu32
+from horayzon_extpar_gb300 import synthetic
+from oracle import api as oracle
+
+pytestmark = pytest.mark.gpu
+
+HORIZON_TOL_DEG = 0.25   # search accuracy of the bracketing method (cpp:577)
+SVF_TOL = 1e-3
+EXACT_DEG = 1e-9
+
+
+def assert_parity(h, s, h_ref, s_ref, min_exact=0.999):
+    d = np.abs(h - h_ref)
+    assert np.mean(d <= HORIZON_TOL_DEG) >= 0.999, "horizon parity %.6f" % np.mean(
+        d <= HORIZON_TOL_DEG)
+    assert np.mean(d <= EXACT_DEG) >= min_exact, "exact fraction %.6f" % np.mean(
+        d <= EXACT_DEG)
+    assert np.abs(s - s_ref).max() <= SVF_TOL
+
+
+@pytest.fixture(scope="module", autouse=True)
+def library():
+    return _lib.load()
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_gpu_matches_reference_golden(name):
+    g = load_golden(name)
+    h, s = horizon_svf_comp_py(*g["inputs"], *g["args"])
+    assert h.shape == g["horizon"].shape and h.dtype == np.float64
+    assert h.flags["C_CONTIGUOUS"] and s.shape == g["skyview"].shape
+    assert_parity(h, s, g["horizon"], g["skyview"])
+    np.testing.assert_allclose(s, g["skyview"], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_gpu_mesh_matches_reference_mesh(name):
+    g = load_golden(name)
+    mlon, mlat, mh, vot = build_mesh(*g["inputs"], g["args"][1])
+    np.testing.assert_array_equal(vot, g["mesh_vot"])
+    np.testing.assert_array_equal(mlon, g["mesh_lon"])
+    np.testing.assert_array_equal(mlat, g["mesh_lat"])
+    np.testing.assert_array_equal(mh, g["mesh_h"])
+
+
+@pytest.mark.parametrize("grid_type", [0, 1])
+def test_gpu_enu32_matches_oracle(small_domain, grid_type):
+    enu, vot = mesh_enu32(*small_domain.inputs(), grid_type)
+    e64, e32, vot_o = oracle.mesh_enu(*small_domain.inputs(), grid_type)
+    np.testing.assert_array_equal(vot, vot_o)
+    assert enu.shape == e32.shape
+    assert np.mean(enu == e32) >= 0.9999
+    ulp = np.spacing(np.abs(e32).astype(np.float32))
+    assert (np.abs(enu - e32) <= ulp).all()
+
+
+CONFIGS = [
+    # (domain kwargs, (num_hori, grid_type, dist_search, ray_org_elev, refine, svf))
+    (dict(edge_km=2.5, box_km=70.0, seed=21), (24, 1, 40000.0, 0.2, 1, 2)),
+    (dict(edge_km=2.5, box_km=70.0, seed=21), (24, 0, 40000.0, 0.2, 1, 1)),
+    (dict(edge_km=1.0, box_km=30.0, seed=22, kind="fbm_ridged", hmin=200.0, hmax=4800.0,
+          hurst=0.7, n_features=0), (36, 1, 15000.0, 0.2, 3, 0)),
+    (dict(edge_km=0.5, box_km=12.0, seed=23, kind="eroded", hmin=500.0, hmax=4200.0,
+          n_features=0), (8, 1, 100000.0, 1.5, 7, 2)),
+    (dict(edge_km=3.0, box_km=90.0, seed=24, lat0_deg=-33.0, lon0_deg=150.0,
+          face_rotation_deg=40.0), (24, 1, 500000.0, 0.2, 1, 2)),
+]
+
+
+@pytest.mark.parametrize("dkw,args", CONFIGS)
+def test_gpu_matches_oracle(dkw, args):
+    d = synthetic.make_domain(**dkw)
+    h, s, st = horizon_svf_comp_py(*d.inputs(), *args, return_stats=True)
+    ho, so, sto = oracle.horizon_svf(*d.inputs(), *args)
+    assert_parity(h, s, ho, so)
+    assert st["n_tri"] == sto["n_tri"] and st["n_mesh_vert"] == sto["n_mesh_vert"]
+    # identical hit decisions imply identical ray counts
+    assert abs(st["num_rays"] - sto["num_rays"]) <= 0.001 * sto["num_rays"]
+
+
+def test_gpu_shuffled_slots(small_domain):
+    """-2 entries anywhere in a vertex's column (slot mapping, not position)."""
+    d = small_domain
+    rng = np.random.default_rng(3)
+    cov = d.cells_of_vertex.copy()
+    for v in range(cov.shape[1]):
+        cov[:, v] = cov[rng.permutation(6), v]
+    inputs = (d.clon, d.clat, d.hsurf, d.vlon, d.vlat, cov)
+    for grid_type in (0, 1):
+        args = (24, grid_type, 30000.0, 0.2, 1, 2)
+        h, s = horizon_svf_comp_py(*inputs, *args)
+        ho, so, _ = oracle.horizon_svf(*inputs, *args)
+        assert_parity(h, s, ho, so)
+
+
+def test_gpu_deterministic(small_domain):
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    a = horizon_svf_comp_py(*small_domain.inputs(), *args)
+    b = horizon_svf_comp_py(*small_domain.inputs(), *args)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_gpu_count_work(small_domain):
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    h, s, st = horizon_svf_comp_py(*small_domain.inputs(), *args, count_work=True,
+                                   return_stats=True)
+    assert st["node_visits"] > st["num_rays"] > 0
+    assert st["tri_tests"] > 0
+
+
+def test_gpu_device_api_equals_host_api(small_domain):
+    torch = pytest.importorskip("torch")
+    from horayzon_extpar_gb300 import horizon_svf_comp_device
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    h, s = horizon_svf_comp_py(*small_domain.inputs(), *args)
+    dev = torch.device("cuda:0")
+    t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in small_domain.inputs()]
+    hd, sd, st = horizon_svf_comp_device(*t, *args)
+    np.testing.assert_array_equal(hd.cpu().numpy(), h)
+    np.testing.assert_array_equal(sd.cpu().numpy(), s)
+
+
+def test_gpu_tiny_and_empty_meshes():
+    d = synthetic.make_domain(edge_km=2.5, box_km=6.0, seed=2)
+    for grid_type in (0, 1):
+        for keep in (1, 2, d.nvertex):
+            cov = d.cells_of_vertex.copy()
+            cov[:, keep:] = -2
+            inputs = (d.clon, d.clat, d.hsurf, d.vlon, d.vlat, cov)
+            args = (24, grid_type, 40000.0, 0.2, 1, 2)
+            h, s = horizon_svf_comp_py(*inputs, *args)
+            ho, so, st = oracle.horizon_svf(*inputs, *args)
+            np.testing.assert_array_equal(h, ho)
+            np.testing.assert_allclose(s, so, atol=1e-12)
+    # no triangles at all: every ray misses, horizon 0, SVF 1
+    cov = np.full_like(d.cells_of_vertex, -2)
+    h, s = horizon_svf_comp_py(d.clon, d.clat, d.hsurf, d.vlon, d.vlat, cov,
+                               24, 1, 40000.0, 0.2, 1, 2)
+    assert (h == 0).all() and (s == 1).all()
+
+
+def test_gpu_bad_index_status():
+    L = _lib.load()
+    d = synthetic.make_domain(edge_km=2.5, box_km=20.0, seed=1)
+    cov = d.cells_of_vertex.copy()
+    cov[2, 5] = d.ncell + 7
+    h = np.empty((24, d.ncell))
+    s = np.empty(d.ncell)
+    D = C.POINTER(C.c_double)
+    rc = L.hz_horizon_svf(d.clon.ctypes.data_as(D), d.clat.ctypes.data_as(D),
+                          d.hsurf.ctypes.data_as(D), d.vlon.ctypes.data_as(D),
+                          d.vlat.ctypes.data_as(D), cov.ctypes.data_as(C.POINTER(C.c_int32)),
+                          h.ctypes.data_as(D), s.ctypes.data_as(D), d.ncell, d.nvertex, 24, 1,
+                          40000.0, 0.2, 1, 2, None, None)
+    assert rc == _lib.HZ_ERR_INDEX
+    assert "out of range" in _lib.last_error()
+    # the library stays usable afterwards
+    h2, s2 = horizon_svf_comp_py(*d.inputs(), 24, 1, 40000.0, 0.2, 1, 2)
+    assert np.isfinite(h2).all()
+
+
+def test_gpu_dropin_c_symbol(small_domain):
+    """horizon_svf_comp: the reference's own signature, C linkage."""
+    L = _lib.load()
+    d = small_domain
+    h = np.empty((24, d.ncell))
+    s = np.empty(d.ncell)
+    D = C.POINTER(C.c_double)
+    L.horizon_svf_comp(d.clon.ctypes.data_as(D), d.clat.ctypes.data_as(D),
+                       d.hsurf.ctypes.data_as(D), d.vlon.ctypes.data_as(D),
+                       d.vlat.ctypes.data_as(D),
+                       d.cells_of_vertex.ctypes.data_as(C.POINTER(C.c_int32)),
+                       h.ctypes.data_as(D), s.ctypes.data_as(D), d.ncell, d.nvertex, 24, 1,
+                       40000.0, 0.2, 1, 2)
+    ho, so = horizon_svf_comp_py(*d.inputs(), 24, 1, 40000.0, 0.2, 1, 2)
+    np.testing.assert_array_equal(h, ho)
+    np.testing.assert_array_equal(s, so)
