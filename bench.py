@@ -1,0 +1,387 @@
+"""Benchmark: horizon evaluations/s of the HORAYZON horizon + SVF path.
+
+One step = one full pass of the hot path over one domain: triangle-mesh
+assembly, geodetic frames, LBVH build and the bracketing horizon search with
+the SVF epilogue (mo_lradtopo_horayzon.cpp:562-785), on the 500 m / 600 x 600
+km / nhori 24 workload (~3.1M cells; grid_type 1, dist_search 40 km,
+ray_org_elev 0.2 m, refine_factor 1, svf_type 2). One horizon evaluation is
+one (cell, azimuth) of the output.
+
+* ``value``: device-resident inputs (hz_horizon_svf_device), CUDA events
+  around each step on the launching stream, L2 flushed (256 MiB write)
+  between steps, max over ranks.
+* ``e2e``: the public host entry (hz_horizon_svf) on pinned host buffers,
+  host->device inputs and device->host outputs inside the timed region.
+* ``roofline``: the horizon-search kernel; algorithmic bytes per launch =
+  64 B per BVH node visit + 48 B per triangle test, counted on the device
+  over the same launch.
+* ``cpu_baseline`` (rank 0, N=1): the CPU oracle on all host cores on a
+  bounded sample (full mesh + BVH build, ray phase on a random cell subset,
+  scaled to the full domain).
+
+``--impl reference`` times the reference's own CPU algorithm on all host
+cores on the same workload and prints the same JSON line. It runs the C
+restatement of the reference (oracle/hz_oracle.c, bit-identical to the
+shim-compiled reference on the golden cases): the reference source is not
+present where this benchmark runs, and the reference entry point cannot time
+a bounded cell sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("horizon evals/s (cells×azimuths) 500 m nhori=24, learned vs plain GPU; "
+          "rays/s")
+WORKLOAD = "500 m ICON-like grid, 600x600 km, fBm(H=0.7)+ridged noise 200-4800 m, nhori=24"
+ARGS = (24, 1, 40000.0, 0.2, 1, 2)  # num_hori, grid_type, dist_search, ray_org_elev, refine, svf
+BYTES_PER_NODE = 64
+BYTES_PER_TRI = 48
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_workload(seed: int, box_km: float):
+    """The 500 m workload; box_km < 600 gives a smaller domain of the same recipe."""
+    from horayzon_extpar_gb300 import synthetic
+    return synthetic.make_config("c3", seed=seed, box_km=box_km)
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """DRAM bytes per launch of the search kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_trace_exact_c3.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"],
+                    "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample_run(dom, target_ray_s: float):
+    """Times the CPU oracle on a bounded sample; returns a dict."""
+    from oracle import api as oracle
+    ncell = dom.ncell
+    nth = os.cpu_count() or 1
+    rng = np.random.default_rng(1234)
+    kind = "port"
+    # Calibrate the ray phase on 2000 cells, then size the sample.
+    cal = rng.choice(ncell, min(2000, ncell), replace=False)
+    _, _, st = oracle.horizon_svf(*dom.inputs(), *ARGS, cells=cal, nthreads=nth)
+    per_cell = max(st["t_rays"], 1e-6) / cal.size
+    n = int(min(ncell, max(2000, target_ray_s / per_cell)))
+    cells = np.sort(rng.choice(ncell, n, replace=False))
+    t0 = time.perf_counter()
+    _, _, st = oracle.horizon_svf(*dom.inputs(), *ARGS, cells=cells, nthreads=nth)
+    wall = time.perf_counter() - t0
+    t_full = st["t_mesh"] + st["t_bvh"] + st["t_rays"] * ncell / n
+    evals = ncell * ARGS[0]
+    rays_full = st["num_rays"] * ncell / n
+    return {"value": evals / t_full, "unit": "evals/s", "cores": nth, "kind": kind,
+            "sample": ("full mesh + BVH build (%.2f s) and the ray phase on %d of %d cells "
+                       "(%.2f s on %d threads), scaled to the full domain"
+                       % (st["t_mesh"] + st["t_bvh"], n, ncell, st["t_rays"], nth)),
+            "rays_per_s": rays_full / t_full, "seconds_full_domain": t_full,
+            "wall_s": wall}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    dom = make_workload(0, args.box_km)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample_run(dom, args.cpu_seconds)
+        if i >= args.warmup:
+            vals.append(r)
+    v = float(np.mean([r["value"] for r in vals]))
+    evals = dom.ncell * ARGS[0]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "evals/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * evals / v, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 rays / f64 frames", "data": "synthetic",
+        "config": {"workload": WORKLOAD if args.box_km == 600.0 else
+                   WORKLOAD.replace("600x600", "%gx%g" % (args.box_km, args.box_km)),
+                   "ncell": dom.ncell, "nvertex": dom.nvertex,
+                   "num_hori": ARGS[0], "grid_type": ARGS[1], "dist_search_m": ARGS[2],
+                   "ray_org_elev_m": ARGS[3], "refine_factor": ARGS[4], "svf_type": ARGS[5]},
+        "cpu_baseline": {"value": v, "unit": "evals/s", "cores": vals[-1]["cores"],
+                         "kind": vals[-1]["kind"], "sample": vals[-1]["sample"]},
+        "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "rays_per_s": float(np.mean([r["rays_per_s"] for r in vals])),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import ctypes as C
+
+    import torch
+
+    from horayzon_extpar_gb300 import _lib, horizon_svf_comp_device
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    L = _lib.load(build_if_missing=True)
+
+    # Each rank solves its own independent domain (weak scaling).
+    dom = make_workload(rank, args.box_km)
+    evals = dom.ncell * ARGS[0]
+    host = [np.ascontiguousarray(a) for a in dom.inputs()]
+    d_in = [torch.from_numpy(a).to(dev) for a in host]
+    horizon = torch.empty((ARGS[0], dom.ncell), dtype=torch.float64, device=dev)
+    skyview = torch.empty(dom.ncell, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(count=False):
+        return horizon_svf_comp_device(*d_in, *ARGS, horizon=horizon, skyview=skyview,
+                                       stream=stream, count_work=count)[2]
+
+    # Untimed: work counters of the same launch (node visits, triangle tests).
+    st_count = step(count=True)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    stats = []
+    with ClockSampler(local) as clk:
+        barrier()
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            ev[k][0].record(stream)
+            stats.append(step())
+            ev[k][1].record(stream)
+        barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = float(np.mean(step_ms))
+    trace_ms = float(np.mean([s["ms_trace"] for s in stats]))
+    if world > 1:
+        t = torch.tensor([ms, trace_ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, trace_ms = float(t[0]), float(t[1])
+    rays = st_count["num_rays"]
+
+    # End to end through the public host entry with pinned buffers.
+    pin = [torch.from_numpy(a).pin_memory() for a in host]
+    h_out = torch.empty((ARGS[0], dom.ncell), dtype=torch.float64).pin_memory()
+    s_out = torch.empty(dom.ncell, dtype=torch.float64).pin_memory()
+    D = C.POINTER(C.c_double)
+    I32 = C.POINTER(C.c_int32)
+    opt = _lib.default_options(device=local)
+    st = _lib.Stats()
+
+    def e2e_step():
+        rc = L.hz_horizon_svf(*(C.cast(t.data_ptr(), D) for t in pin[:5]),
+                              C.cast(pin[5].data_ptr(), I32), C.cast(h_out.data_ptr(), D),
+                              C.cast(s_out.data_ptr(), D), dom.ncell, dom.nvertex, *ARGS,
+                              C.byref(opt), C.byref(st))
+        _lib.check(rc)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e2e_step()
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t[0])
+    h2d = sum(a.nbytes for a in host)
+    d2h = h_out.numel() * 8 + s_out.numel() * 8
+
+    # Check once that the timed outputs are sane (lattice, range).
+    hz = horizon.cpu().numpy()
+    sv = skyview.cpu().numpy()
+    if not (np.isfinite(hz).all() and (sv > 0).all() and (sv <= 1).all()):
+        raise RuntimeError("invalid outputs")
+
+    peak, peak_kind = measured_peaks()
+    alg_bytes = BYTES_PER_NODE * st_count["node_visits"] + BYTES_PER_TRI * st_count["tri_tests"]
+    achieved = alg_bytes / (trace_ms * 1e-3) / 1e9
+    traffic = traffic_from_profile()
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        cpu = cpu_sample_run(dom, args.cpu_seconds)
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    launches = stats[0].get("kernel_launches", None)
+    line = {
+        "metric": METRIC,
+        "value": world * evals / (ms * 1e-3),
+        "unit": "evals/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 rays / f64 frames",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD if args.box_km == 600.0 else
+                   WORKLOAD.replace("600x600", "%gx%g" % (args.box_km, args.box_km)),
+                   "variant": "plain (chained bracketing search)",
+                   "ncell": dom.ncell, "nvertex": dom.nvertex, "n_tri": st_count["n_tri"],
+                   "num_hori": ARGS[0], "grid_type": ARGS[1], "dist_search_m": ARGS[2],
+                   "ray_org_elev_m": ARGS[3], "refine_factor": ARGS[4], "svf_type": ARGS[5],
+                   "evals_per_step": evals, "l2": "256 MiB flush write between steps; "
+                   "per-step working set > 2 GB", "parallelism": "replica per GPU" if world > 1
+                   else "1 GPU"},
+        "rays_per_s": world * rays / (ms * 1e-3),
+        "rays_per_eval": rays / evals,
+        "phase_ms": {"mesh": float(np.mean([s["ms_mesh"] for s in stats])),
+                     "bvh": float(np.mean([s["ms_bvh"] for s in stats])),
+                     "trace": trace_ms},
+        "e2e": {"value": world * evals / e2e_s, "unit": "evals/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"kernel": "k_trace_exact", "bound": "hbm", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "alg_bytes_per_launch": alg_bytes,
+                     "node_visits_per_ray": st_count["node_visits"] / rays,
+                     "tri_tests_per_ray": st_count["tri_tests"] / rays},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": (launches * args.steps) if launches else None,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--box-km", type=float, default=600.0,
+                    help="domain width (600 = the benchmark workload; smaller for profiling)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-seconds", type=float, default=8.0,
+                    help="target seconds of CPU ray work per CPU measurement")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -26,7 +26,12 @@ EXPORTED_SYMBOLS = ("hz_default_options", "horizon_svf_comp", "hz_horizon_svf",
 
 class Options(C.Structure):
     _fields_ = [("size", C.c_int32), ("device", C.c_int32), ("count_work", C.c_int32),
-                ("verbose", C.c_int32), ("elev_floor_deg", C.c_double)]
+                ("verbose", C.c_int32), ("elev_floor_deg", C.c_double),
+                ("cell_begin", C.c_int32), ("cell_count", C.c_int32),
+                ("kernel", C.c_int32), ("advance_min", C.c_int32)]
+
+
+HZ_KERNEL_PERSISTENT, HZ_KERNEL_PER_CELL = 0, 1
 
 
 class Stats(C.Structure):
@@ -35,7 +40,7 @@ class Stats(C.Structure):
                 ("n_mesh_vert", C.c_int32), ("ms_h2d", C.c_double),
                 ("ms_mesh", C.c_double), ("ms_bvh", C.c_double),
                 ("ms_trace", C.c_double), ("ms_d2h", C.c_double),
-                ("ms_total", C.c_double)]
+                ("ms_total", C.c_double), ("kernel_launches", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

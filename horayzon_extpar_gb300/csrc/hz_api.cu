@@ -21,6 +21,7 @@ namespace hz {
 namespace {
 
 thread_local std::string g_last_error;
+thread_local long long g_launches = 0;
 
 int fail(int code, const char* fmt, ...) {
   char buf[512];
@@ -78,6 +79,11 @@ struct Buffers {
   Node* nodes;
   Tri* tris;
   BvhScratch bvh;
+  // cell order of the persistent search
+  int32_t* order;
+  void* order_scratch;
+  unsigned* cell_bounds;
+  int* work;
   // misc
   unsigned long long* counters;  // rays, node visits, triangle tests
   int* err;
@@ -123,6 +129,10 @@ Buffers carve(Carver& c, const Sizes& s) {
   b.bvh.counter = c.take<int>(nt);
   b.bvh.bounds = c.take<unsigned>(16);
   b.bvh.sort_scratch = c.take<char>(radix_scratch_u32(nt));
+  b.order = c.take<int32_t>(s.ncell);
+  b.order_scratch = c.take<char>(cell_order_scratch_bytes(s.ncell));
+  b.cell_bounds = c.take<unsigned>(8);
+  b.work = c.take<int>(4);
   b.counters = c.take<unsigned long long>(4);
   b.err = c.take<int>(4);
   return b;
@@ -268,6 +278,7 @@ int run_pipeline(Engine& E, const Problem& pr, const Buffers& b, cudaStream_t s,
                  const hz_options& opt, hz_stats* st, Stop stop, int* n_tri_out,
                  int* n_mv_out) {
   auto t0 = std::chrono::steady_clock::now();
+  g_launches = 0;
   HZ_CUDA(cudaMemsetAsync(b.err, 0, 4 * sizeof(int), s));
   HZ_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(unsigned long long), s));
   HZ_CUDA(cudaEventRecord(E.ev[0], s));
@@ -328,6 +339,15 @@ int run_pipeline(Engine& E, const Problem& pr, const Buffers& b, cudaStream_t s,
   std::memset(&p, 0, sizeof(p));
   p.cell_enu = b.cell_enu;
   p.ncell = pr.ncell;
+  p.cell_begin = 0;
+  p.cell_count = pr.ncell;
+  if (opt.cell_count > 0) {
+    if (opt.cell_begin < 0 || (long long)opt.cell_begin + opt.cell_count > pr.ncell)
+      return fail(HZ_ERR_VALUE, "cell range [%d, %d) outside [0, %d)", opt.cell_begin,
+                  opt.cell_begin + opt.cell_count, pr.ncell);
+    p.cell_begin = opt.cell_begin;
+    p.cell_count = opt.cell_count;
+  }
   p.nodes = b.nodes;
   p.tris = b.tris;
   p.root = n_tri > 0 ? 0 : kEmptyRef;
@@ -354,7 +374,14 @@ int run_pipeline(Engine& E, const Problem& pr, const Buffers& b, cudaStream_t s,
   p.skyview = pr.skyview;
   p.counters = b.counters;
   p.err = b.err;
-  HZ_CUDA(trace_exact(p, opt.count_work != 0, s));
+  if (opt.kernel == HZ_KERNEL_PER_CELL) {
+    HZ_CUDA(trace_exact(p, opt.count_work != 0, s));
+  } else {
+    const int adv = opt.advance_min >= 1 && opt.advance_min <= 32 ? opt.advance_min : 16;
+    HZ_CUDA(cell_order(b.cell_enu, p.cell_begin, p.cell_count, b.order, b.order_scratch,
+                       b.cell_bounds, b.work, s));
+    HZ_CUDA(trace_flat(p, b.order, b.work, adv, opt.count_work != 0, s));
+  }
   HZ_CUDA(cudaEventRecord(E.ev[3], s));
 
   HZ_CUDA(cudaMemcpyAsync(E.pinned + 8, b.counters, 3 * sizeof(unsigned long long),
@@ -364,6 +391,7 @@ int run_pipeline(Engine& E, const Problem& pr, const Buffers& b, cudaStream_t s,
   const int err1 = (int)(E.pinned[12] & 0xFFFFFFFFull);
   if (err1 & kErrStack) return fail(HZ_ERR_INTERNAL, "BVH traversal stack overflow");
   if (st) {
+    st->kernel_launches = g_launches;
     st->num_rays = (int64_t)E.pinned[8];
     st->node_visits = (int64_t)E.pinned[9];
     st->tri_tests = (int64_t)E.pinned[10];
@@ -399,6 +427,9 @@ hz_options resolve(const hz_options* opt) {
 }
 
 }  // namespace
+
+void note_launches(int n) { g_launches += n; }
+
 }  // namespace hz
 
 using namespace hz;

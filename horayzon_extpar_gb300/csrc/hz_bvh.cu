@@ -251,14 +251,17 @@ cudaError_t bvh_build(const float* vert32, const int* vot, int n, Node* nodes, T
   k_init_bounds<<<1, 1, 0, s>>>(sc.bounds);
   k_tri_bounds<<<grid_for(n, 256), 256, 0, s>>>(vert32, vot, n, sc.cxy, sc.bounds);
   k_morton<<<grid_for(n, 256), 256, 0, s>>>(sc.cxy, n, sc.bounds, sc.keys, sc.vals);
+  note_launches(3);
   cudaError_t e = radix_sort_pairs(sc.keys, sc.vals, sc.keys_alt, sc.vals_alt, n, 32,
                                    sc.sort_scratch, s);
   if (e != cudaSuccess) return e;
   k_gather<<<grid_for(n, 256), 256, 0, s>>>(vert32, vot, sc.vals, n, tris);
   if (n <= kLeafMax) {
     k_small_root<<<1, 1, 0, s>>>(nodes, tris, n, sc.bounds);
+    note_launches(2);
     return cudaGetLastError();
   }
+  note_launches(3);
   k_karras<<<grid_for(n - 1, 256), 256, 0, s>>>(sc.keys, n, nodes, sc.parent, sc.nsize,
                                                 sc.counter);
   k_refit<<<grid_for(n - 1, 256), 256, 0, s>>>(nodes, tris, n, sc.parent, sc.nsize,

@@ -10,6 +10,9 @@
 
 namespace hz {
 
+// Kernel-launch accounting of the calling thread (reported in hz_stats).
+void note_launches(int n);
+
 // ---- hz_scan_sort.cu -------------------------------------------------------
 // Exclusive prefix sum of n values; total to *d_total (device). `partials`
 // needs scan_partials(n) elements.
@@ -70,7 +73,8 @@ cudaError_t bvh_build(const float* vert32, const int* vot, int n_tri, Node* node
 // ---- hz_trace.cu ------------------------------------------------------------
 struct TraceParams {
   const double* cell_enu;   // [3 * ncell] FP64 ENU of cell centres
-  int ncell;
+  int ncell;                // row stride of horizon
+  int cell_begin, cell_count;  // cells traced: [cell_begin, cell_begin + cell_count)
   const Node* nodes;
   const Tri* tris;
   int root;                 // 0, or kEmptyRef for an empty mesh
@@ -85,6 +89,16 @@ struct TraceParams {
   unsigned long long* counters;  // [0] rays, [1] node visits, [2] triangle tests
   int* err;
 };
+// One thread per cell, nested loops as in the reference (simple; kept as the
+// second implementation the flattened kernel is tested against).
 cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s);
+// Morton order of cells [begin, begin + count) into order[count]; also resets
+// the work counter used by trace_flat.
+size_t cell_order_scratch_bytes(long long n);
+cudaError_t cell_order(const double* cell_enu, int begin, int count, int32_t* order,
+                       void* scratch, unsigned* bounds, int* work, cudaStream_t s);
+// Persistent flattened search (same rays and results as trace_exact).
+cudaError_t trace_flat(const TraceParams& p, const int32_t* order, int* work,
+                       int advance_min, bool count_work, cudaStream_t s);
 
 }  // namespace hz

@@ -213,6 +213,7 @@ cudaError_t mesh_count(const int* cov, int nv, int ncell, int grid_type,
                        unsigned long long* packed, int* err, cudaStream_t s) {
   if (nv <= 0) return cudaSuccess;
   k_mesh_count<<<grid_for(nv, 256), 256, 0, s>>>(cov, nv, ncell, grid_type, packed, err);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -225,6 +226,7 @@ cudaError_t mesh_emit(const double* clon, const double* clat, const double* hsur
   k_mesh_emit<<<grid_for(nv, 128), 128, 0, s>>>(clon, clat, hsurf, vlon, vlat, cov, nv,
                                                 ncell, grid_type, offsets, vot, add_lon,
                                                 add_lat, add_h);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -238,6 +240,7 @@ cudaError_t mesh_ecef(const double* clon, const double* clat, const double* hsur
   k_mesh_ecef<<<nb, kEcefThreads, 0, s>>>(clon, clat, hsurf, add_lon, add_lat, add_h, ncell,
                                           nadd, ecef, block_sums);
   k_sum_blocks<<<1, 1024, 0, s>>>(block_sums, nb, d_origin_sum);
+  note_launches(2);
   return cudaGetLastError();
 }
 
@@ -245,6 +248,7 @@ cudaError_t mesh_enu(const double* ecef, int nmv, int ncell, const Frame& f, flo
                      double* cell_enu, cudaStream_t s) {
   if (nmv <= 0) return cudaSuccess;
   k_mesh_enu<<<grid_for(nmv, 256), 256, 0, s>>>(ecef, nmv, ncell, f, vert32, cell_enu);
+  note_launches(1);
   return cudaGetLastError();
 }
 

@@ -107,6 +107,7 @@ cudaError_t scan_impl(const T* in, T* out, long long n, T* d_total, T* partials,
   k_tile_reduce<T><<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, partials);
   k_partials_scan<T><<<1, kScanThreads, 0, s>>>(partials, nb, d_total);
   k_tile_scan<T><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, partials);
+  note_launches(3);
   return cudaGetLastError();
 }
 
@@ -218,6 +219,7 @@ cudaError_t radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_alt,
     if (e != cudaSuccess) return e;
     k_rs_scatter<<<(unsigned)ntiles, kRsThreads, 0, s>>>(ki, vi, ko, vo, n, shift, offs,
                                                          ntiles);
+    note_launches(2);
     uint32_t* tk = ki; ki = ko; ko = tk;
     int32_t* tv = vi; vi = vo; vo = tv;
   }

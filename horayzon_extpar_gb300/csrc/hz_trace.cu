@@ -193,9 +193,10 @@ __device__ __forceinline__ V3 rotate3(V3 v, V3 k, double s, double c) {
 
 template <bool kCount>
 __global__ void __launch_bounds__(128) k_trace_exact(TraceParams p) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = p.cell_begin + k;
   unsigned long long rays = 0, nvis = 0, ntest = 0;
-  if (i < p.ncell) {
+  if (k < p.cell_count) {
     const V3 q{p.cell_enu[3LL * i], p.cell_enu[3LL * i + 1], p.cell_enu[3LL * i + 2]};
     V3 normal{q.x - p.centre.x, q.y - p.centre.y, q.z - p.centre.z};
     unit3(normal);
@@ -272,12 +273,312 @@ __global__ void __launch_bounds__(128) k_trace_exact(TraceParams p) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Persistent, flattened variant. Same search and the same rays as
+// k_trace_exact, restructured for SIMT efficiency: every loop iteration runs
+// one traversal step (one BVH node or one leaf) for all lanes; a lane whose
+// ray has finished advances its cell's search state machine (next elevation,
+// next azimuth or next cell) only once at least `advance_min` lanes of the
+// warp are waiting, so the FP64 search code runs for many lanes at once.
+// Lanes take cells from a global counter in the order given by `order`
+// (Morton order of the cells), and keep their FP64 search state in shared
+// memory to leave registers to the traversal.
+// ---------------------------------------------------------------------------
+constexpr int kFlatBlock = 128;
+
+enum : int { kPhaseFirst = 0, kPhaseUp = 1, kPhaseDown = 2 };
+
+template <bool kCount>
+__global__ void __launch_bounds__(kFlatBlock, 8)
+    k_trace_flat(TraceParams p, const int* __restrict__ order, int* __restrict__ work,
+                 int advance_min) {
+  // 0-2 sphere normal, 3-5 ray direction, 6-8 elevation axis,
+  // 9 elevation, 10 sector sum, 11 SVF sum
+  __shared__ double sv[12][kFlatBlock];
+  const int t = threadIdx.x;
+  const double ha = p.hori_acc;
+
+  int cell = -1, a = 0, phase = kPhaseFirst, up = 0;
+  bool need = true, start = true, last_hit = false;
+  int ref = kEmptyRef, sp = 0;
+  int stack[kStackDepth];
+  float ox = 0.f, oy = 0.f, oz = 0.f;
+  Ray r;
+  unsigned long long rays = 0, nvis = 0, ntest = 0;
+
+  for (;;) {
+    const unsigned act = __activemask();
+    const unsigned waiting = __ballot_sync(act, need);
+    if (need && (__popc(waiting) >= advance_min || waiting == act)) {
+      bool emit = false, alive = true;
+      while (!emit) {
+        if (start) {
+          const int k = atomicAdd(work, 1);
+          if (k >= p.cell_count) {
+            alive = false;
+            break;
+          }
+          cell = order ? order[k] : p.cell_begin + k;
+          const V3 q{p.cell_enu[3LL * cell], p.cell_enu[3LL * cell + 1],
+                     p.cell_enu[3LL * cell + 2]};
+          V3 normal{q.x - p.centre.x, q.y - p.centre.y, q.z - p.centre.z};
+          unit3(normal);
+          const V3 v_n{p.pole.x - q.x, p.pole.y - q.y, p.pole.z - q.z};
+          const double dp = dot3(v_n, normal);
+          V3 north{v_n.x - dp * normal.x, v_n.y - dp * normal.y, v_n.z - dp * normal.z};
+          unit3(north);
+          ox = (float)(q.x + normal.x * p.ray_org_elev);
+          oy = (float)(q.y + normal.y * p.ray_org_elev);
+          oz = (float)(q.z + normal.z * p.ray_org_elev);
+          const V3 dir = rotate3(north, normal, p.shift_sin, p.shift_cos);
+          V3 axis = cross3(dir, normal);
+          unit3(axis);
+          sv[0][t] = normal.x; sv[1][t] = normal.y; sv[2][t] = normal.z;
+          sv[3][t] = dir.x; sv[4][t] = dir.y; sv[5][t] = dir.z;
+          sv[6][t] = axis.x; sv[7][t] = axis.y; sv[8][t] = axis.z;
+          sv[9][t] = 0.0; sv[10][t] = 0.0; sv[11][t] = 0.0;
+          a = 0;
+          phase = kPhaseFirst;
+          start = false;
+          emit = true;
+          break;
+        }
+        // Result of the last ray: continue the bracket or close the azimuth.
+        V3 dir{sv[3][t], sv[4][t], sv[5][t]};
+        double elev = sv[9][t];
+        if (phase == kPhaseFirst) {
+          phase = last_hit ? kPhaseUp : kPhaseDown;
+          up = 0;
+        }
+        const bool step_up = phase == kPhaseUp && last_hit && up < kMaxUpSteps;
+        const bool step_dn = phase == kPhaseDown && !last_hit && elev > p.elev_floor;
+        if (step_up || step_dn) {
+          const V3 axis{sv[6][t], sv[7][t], sv[8][t]};
+          if (step_up) {
+            up++;
+            elev += (2.0 * ha);
+            dir = rotate3(dir, axis, p.elev_sin_2ha, p.elev_cos_2ha);
+          } else {
+            elev -= (2.0 * ha);
+            dir = rotate3(dir, axis, -p.elev_sin_2ha, p.elev_cos_2ha);
+          }
+          sv[3][t] = dir.x; sv[4][t] = dir.y; sv[5][t] = dir.z;
+          sv[9][t] = elev;
+          emit = true;
+          break;
+        }
+        double h = phase == kPhaseUp ? elev - ha : elev + ha;
+        const V3 normal{sv[0][t], sv[1][t], sv[2][t]};
+        dir = rotate3(dir, normal, -p.azim_sin, p.azim_cos);
+        if (h < 0.0) h = 0.0;
+        double sector = sv[10][t] + h;
+        if ((a + 1) % p.refine == 0) {
+          p.horizon[(long long)(a / p.refine) * p.ncell + cell] =
+              ((sector / kPi) * 180.0) / (double)p.refine;
+          sector = 0.0;
+        }
+        const double s = sin(h);
+        double svf = sv[11][t];
+        if (p.svf_type == 0) svf += (1.0 - s);
+        else if (p.svf_type == 1) svf += (1.0 - (s * s));
+        else svf += (1.0 - (s * s * s));
+        a++;
+        if (a == p.L) {
+          p.skyview[cell] = svf / (double)p.L;
+          start = true;
+          continue;
+        }
+        sv[10][t] = sector;
+        sv[11][t] = svf;
+        V3 axis = cross3(dir, normal);
+        unit3(axis);
+        sv[3][t] = dir.x; sv[4][t] = dir.y; sv[5][t] = dir.z;
+        sv[6][t] = axis.x; sv[7][t] = axis.y; sv[8][t] = axis.z;
+        phase = kPhaseFirst;
+        emit = true;
+      }
+      if (!alive) break;
+      r = make_ray(ox, oy, oz, (float)sv[3][t], (float)sv[4][t], (float)sv[5][t], p.tfar);
+      ref = p.root;
+      sp = 0;
+      need = false;
+      rays++;
+    }
+    if (need) continue;
+
+    // One traversal step: one internal node or one leaf.
+    bool fin = false, hit = false;
+    if (ref >= 0) {
+      if (kCount) nvis++;
+      const Node* nd = p.nodes + ref;
+      const float4 na = __ldg(&nd->a);
+      const float4 nb = __ldg(&nd->b);
+      const float4 nc = __ldg(&nd->c);
+      const float4 ndd = __ldg(&nd->d);
+      const int c0 = __float_as_int(ndd.x), c1 = __float_as_int(ndd.y);
+      float t0, t1;
+      const bool h0 = box_hit(r, na.x, na.y, na.z, na.w, nc.x, nc.y, t0);
+      const bool h1 = c1 != kEmptyRef && box_hit(r, nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, t1);
+      if (h0 && h1) {
+        if (sp >= kStackDepth) {
+          atomicOr(p.err, kErrStack);
+          fin = true;
+          hit = true;
+        } else {
+          const bool near0 = t0 <= t1;
+          stack[sp++] = near0 ? c1 : c0;
+          ref = near0 ? c0 : c1;
+        }
+      } else if (h0) {
+        ref = c0;
+      } else if (h1) {
+        ref = c1;
+      } else {
+        ref = sp > 0 ? stack[--sp] : kEmptyRef;
+      }
+    } else if (ref != kEmptyRef) {
+      const int s0 = leaf_start(ref), cnt = leaf_count(ref);
+      for (int k = s0; k < s0 + cnt; k++) {
+        if (kCount) ntest++;
+        const float4 v0 = __ldg(&p.tris[k].v0);
+        const float4 v1 = __ldg(&p.tris[k].v1);
+        const float4 v2 = __ldg(&p.tris[k].v2);
+        if (tri_hit(r, v0, v1, v2)) {
+          hit = true;
+          break;
+        }
+      }
+      if (hit) fin = true;
+      else ref = sp > 0 ? stack[--sp] : kEmptyRef;
+    }
+    if (!fin && ref == kEmptyRef) fin = true;
+    if (fin) {
+      need = true;
+      last_hit = hit;
+    }
+  }
+  rays = warp_sum_u64(rays);
+  if (kCount) {
+    nvis = warp_sum_u64(nvis);
+    ntest = warp_sum_u64(ntest);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&p.counters[0], rays);
+    if (kCount) {
+      atomicAdd(&p.counters[1], nvis);
+      atomicAdd(&p.counters[2], ntest);
+    }
+  }
+}
+
+// Morton keys (2 x 16 bits) of the traced cells' horizontal ENU position.
+__global__ void k_cell_bounds(const double* __restrict__ cell_enu, int begin, int count,
+                              unsigned* __restrict__ bounds) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = k < count;
+  const float x = valid ? (float)cell_enu[3LL * (begin + k)] : 0.f;
+  const float y = valid ? (float)cell_enu[3LL * (begin + k) + 1] : 0.f;
+  unsigned mnx = valid ? f2ord(x) : 0xFFFFFFFFu, mny = valid ? f2ord(y) : 0xFFFFFFFFu;
+  unsigned mxx = valid ? f2ord(x) : 0u, mxy = valid ? f2ord(y) : 0u;
+  mnx = __reduce_min_sync(0xffffffffu, mnx);
+  mny = __reduce_min_sync(0xffffffffu, mny);
+  mxx = __reduce_max_sync(0xffffffffu, mxx);
+  mxy = __reduce_max_sync(0xffffffffu, mxy);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&bounds[0], mnx);
+    atomicMin(&bounds[1], mny);
+    atomicMax(&bounds[2], mxx);
+    atomicMax(&bounds[3], mxy);
+  }
+}
+
+__device__ __forceinline__ uint32_t spread16(uint32_t x) {
+  x &= 0x0000FFFFu;
+  x = (x | (x << 8)) & 0x00FF00FFu;
+  x = (x | (x << 4)) & 0x0F0F0F0Fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+
+__global__ void k_cell_keys(const double* __restrict__ cell_enu, int begin, int count,
+                            const unsigned* __restrict__ bounds, uint32_t* __restrict__ keys,
+                            int32_t* __restrict__ vals) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const float mnx = ord2f(bounds[0]), mny = ord2f(bounds[1]);
+  const float ex = ord2f(bounds[2]) - mnx, ey = ord2f(bounds[3]) - mny;
+  const float x = (float)cell_enu[3LL * (begin + k)];
+  const float y = (float)cell_enu[3LL * (begin + k) + 1];
+  const float fx = ex > 0.f ? (x - mnx) * (65535.0f / ex) : 0.f;
+  const float fy = ey > 0.f ? (y - mny) * (65535.0f / ey) : 0.f;
+  const uint32_t qx = fx <= 0.f ? 0u : (fx >= 65535.0f ? 65535u : (uint32_t)fx);
+  const uint32_t qy = fy <= 0.f ? 0u : (fy >= 65535.0f ? 65535u : (uint32_t)fy);
+  keys[k] = spread16(qx) | (spread16(qy) << 1);
+  vals[k] = begin + k;
+}
+
+__global__ void k_init_cell_bounds(unsigned* b, int* work) {
+  b[0] = 0xFFFFFFFFu;
+  b[1] = 0xFFFFFFFFu;
+  b[2] = 0u;
+  b[3] = 0u;
+  *work = 0;
+}
+
 }  // namespace
 
+size_t cell_order_scratch_bytes(long long n) {
+  if (n < 1) n = 1;
+  return 4 * sizeof(uint32_t) * (size_t)n + radix_scratch_u32(n) + 64 + 5 * 256;
+}
+
+cudaError_t cell_order(const double* cell_enu, int begin, int count, int32_t* order,
+                       void* scratch, unsigned* bounds, int* work, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  char* base = (char*)scratch;
+  auto take = [&](size_t bytes) {
+    char* q = base;
+    base += (bytes + 255) & ~size_t(255);
+    return (void*)q;
+  };
+  uint32_t* keys = (uint32_t*)take(sizeof(uint32_t) * count);
+  uint32_t* keys_alt = (uint32_t*)take(sizeof(uint32_t) * count);
+  int32_t* vals_alt = (int32_t*)take(sizeof(int32_t) * count);
+  void* sort_scratch = take(radix_scratch_u32(count));
+  k_init_cell_bounds<<<1, 1, 0, s>>>(bounds, work);
+  k_cell_bounds<<<grid_for(count, 256), 256, 0, s>>>(cell_enu, begin, count, bounds);
+  k_cell_keys<<<grid_for(count, 256), 256, 0, s>>>(cell_enu, begin, count, bounds, keys, order);
+  note_launches(3);
+  return radix_sort_pairs(keys, order, keys_alt, vals_alt, count, 32, sort_scratch, s);
+}
+
+cudaError_t trace_flat(const TraceParams& p, const int32_t* order, int* work,
+                       int advance_min, bool count_work, cudaStream_t s) {
+  if (p.cell_count <= 0) return cudaSuccess;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (count_work)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_flat<true>, kFlatBlock, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_flat<false>, kFlatBlock, 0);
+  long long blocks = (long long)sms * (per_sm > 0 ? per_sm : 1);
+  const long long needed = (p.cell_count + kFlatBlock - 1) / kFlatBlock;
+  if (blocks > needed) blocks = needed;
+  if (count_work)
+    k_trace_flat<true><<<(unsigned)blocks, kFlatBlock, 0, s>>>(p, order, work, advance_min);
+  else
+    k_trace_flat<false><<<(unsigned)blocks, kFlatBlock, 0, s>>>(p, order, work, advance_min);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
 cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s) {
-  if (p.ncell <= 0) return cudaSuccess;
-  if (count_work) k_trace_exact<true><<<grid_for(p.ncell, 128), 128, 0, s>>>(p);
-  else k_trace_exact<false><<<grid_for(p.ncell, 128), 128, 0, s>>>(p);
+  if (p.cell_count <= 0) return cudaSuccess;
+  if (count_work) k_trace_exact<true><<<grid_for(p.cell_count, 128), 128, 0, s>>>(p);
+  else k_trace_exact<false><<<grid_for(p.cell_count, 128), 128, 0, s>>>(p);
+  note_launches(1);
   return cudaGetLastError();
 }
 

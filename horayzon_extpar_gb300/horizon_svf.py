@@ -71,24 +71,32 @@ def _check_args(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_t
         raise ValueError("'svf_type' must be in the range [0, 2]")
 
 
-def _options(device, count_work, elev_floor_deg, verbose):
+def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
+             advance_min=0):
+    begin, count = (0, 0) if cells is None else (int(cells[0]), int(cells[1]) - int(cells[0]))
     return _lib.default_options(device=int(device), count_work=int(bool(count_work)),
                                 elev_floor_deg=float(elev_floor_deg),
-                                verbose=int(bool(verbose)))
+                                verbose=int(bool(verbose)), cell_begin=begin,
+                                cell_count=count, kernel=int(kernel),
+                                advance_min=int(advance_min))
 
 
 def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori,
                         grid_type, dist_search, ray_org_elev, refine_factor, svf_type,
                         *, device=-1, count_work=False, elev_floor_deg=-85.0,
-                        verbose=False, return_stats=False):
+                        verbose=False, return_stats=False, cells=None, kernel=0,
+                        advance_min=0):
     """Compute the terrain horizon and sky view factor on the GPU.
 
     Arguments and returns as horizon_svf.pyx:15-76: FP64 1-D ``clon, clat``
     [rad], ``hsurf`` [m], ``vlon, vlat`` [rad]; int32 (6, nvertex)
     ``cells_of_vertex`` (-2 = no cell); returns ``horizon`` (num_hori, ncell)
     [deg] and ``skyview`` (ncell) as new C-order float64 arrays. Keyword-only
-    extras: CUDA ``device``, work counters, the downward-walk bound and, with
-    ``return_stats``, a third return value with ray counts and phase times.
+    extras: CUDA ``device``, work counters, the downward-walk bound, a cell
+    range ``cells=(begin, end)`` to trace (entries outside it are NaN), the
+    search ``kernel`` (0 persistent, 1 one thread per cell) and its
+    ``advance_min`` knob and, with ``return_stats``, a third return value
+    with ray counts and phase times.
     """
     clon = _typed("clon", clon, np.float64, 1)
     clat = _typed("clat", clat, np.float64, 1)
@@ -106,11 +114,14 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
 
     horizon = np.empty((num_hori, clon.size), dtype=np.float64)
     skyview = np.empty(clon.size, dtype=np.float64)
+    if cells is not None:
+        horizon.fill(np.nan)
+        skyview.fill(np.nan)
     clon, clat, hsurf, vlon, vlat = (np.ascontiguousarray(a) for a in
                                      (clon, clat, hsurf, vlon, vlat))
     cells_of_vertex = np.ascontiguousarray(cells_of_vertex)
     L = _lib.load()
-    opt = _options(device, count_work, elev_floor_deg, verbose)
+    opt = _options(device, count_work, elev_floor_deg, verbose, cells, kernel, advance_min)
     st = _lib.Stats()
     rc = L.hz_horizon_svf(clon.ctypes.data_as(_D), clat.ctypes.data_as(_D),
                           hsurf.ctypes.data_as(_D), vlon.ctypes.data_as(_D),
@@ -128,12 +139,15 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
 def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori,
                             grid_type, dist_search, ray_org_elev, refine_factor,
                             svf_type, horizon=None, skyview=None, *, stream=None,
-                            count_work=False, elev_floor_deg=-85.0):
+                            count_work=False, elev_floor_deg=-85.0, cells=None, kernel=0,
+                            advance_min=0):
     """Same computation on CUDA tensors (torch) already resident on one GPU.
 
     Inputs: contiguous float64 / int32 tensors on the same device, layouts as
     in :func:`horizon_svf_comp_py`. ``horizon``/``skyview`` may be passed
-    preallocated. Runs on ``stream`` (default: torch's current stream) and
+    preallocated. ``cells=(begin, end)`` traces only that cell range (the
+    mesh and BVH always cover the whole domain; other output entries are left
+    untouched). Runs on ``stream`` (default: torch's current stream) and
     returns ``(horizon, skyview, stats)``.
     """
     import torch
@@ -162,7 +176,7 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
         stream = torch.cuda.current_stream(dev)
     L = _lib.load()
     opt = _options(dev.index if dev.index is not None else -1, count_work,
-                   elev_floor_deg, False)
+                   elev_floor_deg, False, cells, kernel, advance_min)
     st = _lib.Stats()
     rc = L.hz_horizon_svf_device(clon.data_ptr(), clat.data_ptr(), hsurf.data_ptr(),
                                  vlon.data_ptr(), vlat.data_ptr(),

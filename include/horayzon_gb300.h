@@ -48,7 +48,18 @@ typedef struct hz_options {
     int32_t verbose;         /* 1: print the reference's progress lines to stdout */
     double elev_floor_deg;   /* lower bound of the downward elevation walk; the
                                 reference's is -85 (mo_lradtopo_horayzon.cpp:578) */
+    int32_t cell_begin;      /* trace only cells [cell_begin, cell_begin + cell_count); */
+    int32_t cell_count;      /* cell_count <= 0: all cells. Other entries of horizon /
+                                skyview are left untouched (multi-GPU cell shards). */
+    int32_t kernel;          /* HZ_KERNEL_PERSISTENT (default) or HZ_KERNEL_PER_CELL */
+    int32_t advance_min;     /* persistent kernel: lanes of a warp that must wait before
+                                the search state advances (1..32; 0 = library default) */
 } hz_options;
+
+enum {
+    HZ_KERNEL_PERSISTENT = 0,  /* flattened persistent search, Morton-ordered cells */
+    HZ_KERNEL_PER_CELL = 1     /* one thread per cell, nested loops */
+};
 
 typedef struct hz_stats {
     int64_t num_rays;        /* rays cast (reference prints it, cpp:769) */
@@ -62,6 +73,7 @@ typedef struct hz_stats {
     double ms_trace;         /* horizon search + SVF */
     double ms_d2h;           /* device->host copies (host entry points) */
     double ms_total;         /* whole call, wall clock */
+    int64_t kernel_launches; /* CUDA kernels this call launched */
 } hz_stats;
 
 /* Fills *opt with the defaults (device -1, elev_floor_deg -85, counters off). */

@@ -186,3 +186,29 @@ def test_gpu_dropin_c_symbol(small_domain):
     ho, so = horizon_svf_comp_py(*d.inputs(), 24, 1, 40000.0, 0.2, 1, 2)
     np.testing.assert_array_equal(h, ho)
     np.testing.assert_array_equal(s, so)
+
+
+@pytest.mark.parametrize("advance_min", [1, 8, 16, 32])
+def test_gpu_persistent_equals_per_cell(small_domain, advance_min):
+    """The flattened persistent search casts the same rays as the per-cell one."""
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    h1, s1, st1 = horizon_svf_comp_py(*small_domain.inputs(), *args, kernel=1,
+                                      count_work=True, return_stats=True)
+    h2, s2, st2 = horizon_svf_comp_py(*small_domain.inputs(), *args, kernel=0,
+                                      advance_min=advance_min, count_work=True,
+                                      return_stats=True)
+    np.testing.assert_array_equal(h1, h2)
+    np.testing.assert_array_equal(s1, s2)
+    assert st1["num_rays"] == st2["num_rays"]
+    assert st1["tri_tests"] > 0 and st2["tri_tests"] > 0
+
+
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_gpu_cell_range(small_domain, kernel):
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    h, s = horizon_svf_comp_py(*small_domain.inputs(), *args, kernel=kernel)
+    b, e = 100, 700
+    hr, sr = horizon_svf_comp_py(*small_domain.inputs(), *args, kernel=kernel, cells=(b, e))
+    np.testing.assert_array_equal(hr[:, b:e], h[:, b:e])
+    np.testing.assert_array_equal(sr[b:e], s[b:e])
+    assert np.isnan(sr[:b]).all() and np.isnan(sr[e:]).all()
