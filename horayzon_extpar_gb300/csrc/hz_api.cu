@@ -550,9 +550,17 @@ int hz_horizon_svf(const double* clon, const double* clat, const double* hsurf,
   rc = run_pipeline(*E, pr, b, s, opt, stats, Stop::kFull, &ntri, &nmv);
   if (rc) return rc;
   HZ_CUDA(cudaEventRecord(E->ev[6], s));
-  HZ_CUDA(cudaMemcpyAsync(horizon, b.horizon, (size_t)num_hori * nc * 8,
-                          cudaMemcpyDeviceToHost, s));
-  HZ_CUDA(cudaMemcpyAsync(skyview, b.skyview, nc * 8, cudaMemcpyDeviceToHost, s));
+  if (opt.cell_count > 0) {
+    // Only the traced columns: the caller's other entries stay untouched.
+    const size_t c0 = (size_t)opt.cell_begin, cn = (size_t)opt.cell_count;
+    HZ_CUDA(cudaMemcpy2DAsync(horizon + c0, nc * 8, b.horizon + c0, nc * 8, cn * 8,
+                              (size_t)num_hori, cudaMemcpyDeviceToHost, s));
+    HZ_CUDA(cudaMemcpyAsync(skyview + c0, b.skyview + c0, cn * 8, cudaMemcpyDeviceToHost, s));
+  } else {
+    HZ_CUDA(cudaMemcpyAsync(horizon, b.horizon, (size_t)num_hori * nc * 8,
+                            cudaMemcpyDeviceToHost, s));
+    HZ_CUDA(cudaMemcpyAsync(skyview, b.skyview, nc * 8, cudaMemcpyDeviceToHost, s));
+  }
   HZ_CUDA(cudaEventRecord(E->ev[7], s));
   HZ_CUDA(cudaStreamSynchronize(s));
   if (stats) {
