@@ -77,7 +77,7 @@ def measured_peaks():
 
 def traffic_from_profile():
     """DRAM bytes per launch of the search kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_trace_exact_c3.md")
+    path = os.path.join(ROOT, "profiles", "k_trace_flat_c3_500m.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -350,7 +350,7 @@ def run_gpu(args):
                      "trace": trace_ms},
         "e2e": {"value": world * evals / e2e_s, "unit": "evals/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "roofline": {"kernel": "k_trace_exact", "bound": "hbm", "achieved": achieved,
+        "roofline": {"kernel": "k_trace_flat", "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
                      "alg_bytes_per_launch": alg_bytes,
