@@ -21,7 +21,8 @@ HZ_OK, HZ_ERR_VALUE, HZ_ERR_TYPE, HZ_ERR_INDEX, HZ_ERR_CUDA, HZ_ERR_INTERNAL = r
 #: Every symbol include/horayzon_gb300.h declares.
 EXPORTED_SYMBOLS = ("hz_default_options", "horizon_svf_comp", "hz_horizon_svf",
                     "hz_horizon_svf_device", "hz_build_mesh", "hz_mesh_enu32",
-                    "hz_last_error", "hz_version", "hz_release_workspace")
+                    "hz_last_error", "hz_version", "hz_release_workspace",
+                    "hz_horizon_svf_device_static")
 
 
 class Options(C.Structure):
@@ -93,6 +94,8 @@ def load(build_if_missing: bool = True):
         L.hz_horizon_svf_device.argtypes = ([C.c_void_p] * 8 + common +
                                             [C.c_void_p, C.POINTER(Options),
                                              C.POINTER(Stats)])
+        L.hz_horizon_svf_device_static.restype = C.c_int
+        L.hz_horizon_svf_device_static.argtypes = [C.c_void_p] * 8 + common + [C.c_void_p]
         L.hz_build_mesh.restype = C.c_int
         L.hz_build_mesh.argtypes = [_D, _D, _D, _D, _D, _I, C.c_int, C.c_int, C.c_int,
                                     _D, _D, _D, C.c_int, _I, C.c_int,

@@ -430,6 +430,8 @@ hz_options resolve(const hz_options* opt) {
 
 void note_launches(int n) { g_launches += n; }
 
+void set_last_error(const char* msg) { g_last_error = msg; }
+
 }  // namespace hz
 
 using namespace hz;

@@ -12,6 +12,8 @@ namespace hz {
 
 // Kernel-launch accounting of the calling thread (reported in hz_stats).
 void note_launches(int n);
+// Sets the calling thread's message returned by hz_last_error().
+void set_last_error(const char* msg);
 
 // ---- hz_scan_sort.cu -------------------------------------------------------
 // Exclusive prefix sum of n values; total to *d_total (device). `partials`

@@ -151,6 +151,32 @@ int hz_mesh_enu32(const double* clon, const double* clat, const double* hsurf,
                   int32_t* vertex_of_triangle, int cap_tri,
                   int* n_mesh_vert, int* n_tri, int device);
 
+/*
+ * No counterpart in the reference. The same computation as
+ * hz_horizon_svf_device (device pointers, `stream` a cudaStream_t or NULL)
+ * for callers that cannot allocate GPU memory -- for example a model whose
+ * device memory is all owned by another allocator, or a time-stepping code
+ * on a shared GPU that cannot afford the device-wide synchronisation of
+ * cudaMalloc/cudaFree. It allocates nothing: all intermediate data lives in
+ * one fixed 64 MiB __device__ array inside the library (held by every GPU
+ * that loads it until the process exits), which limits a domain to about
+ * 100,000 cells; larger domains are rejected with HZ_ERR_VALUE and a message
+ * naming the limit. The first call on a device resolves the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture. All calls share the array: calls whose GPU
+ * work overlapped would race on it, so the function serialises its callers
+ * and returns after its work on `stream` has finished. The down-walk bound is
+ * the reference's -85 deg; errors are reported through hz_last_error().
+ */
+int hz_horizon_svf_device_static(const double* clon, const double* clat,
+                                 const double* hsurf, const double* vlon,
+                                 const double* vlat, const int32_t* cells_of_vertex,
+                                 double* horizon, double* skyview,
+                                 int num_cell, int num_vertex, int num_hori,
+                                 int grid_type, double dist_search,
+                                 double ray_org_elev, int refine_factor, int svf_type,
+                                 void* stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* hz_last_error(void);
 

@@ -1,0 +1,93 @@
+"""The C ABI library loads without a GPU and exports every function that
+include/horayzon_gb300.h declares; the Python layer raises the reference's
+exceptions before reaching the library (CPU only, no compute calls)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from horayzon_extpar_gb300 import _lib, horizon_svf_comp_py, synthetic
+
+
+def declared_functions():
+    names = []
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not h.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b([a-z_][a-z0-9_]*)\s*\(", src,
+                            flags=re.M)
+    return sorted(set(n for n in names if n not in ("if", "while", "for", "sizeof")))
+
+
+def test_header_declares_expected_entry_points():
+    names = declared_functions()
+    assert set(names) == set(_lib.EXPORTED_SYMBOLS), names
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.load()
+    for name in declared_functions():
+        assert hasattr(L, name), name
+    assert L.hz_version() == 100
+
+
+@pytest.fixture(scope="module")
+def dom():
+    return synthetic.make_domain(edge_km=5.0, box_km=40.0, seed=1)
+
+
+ARGS = (24, 1, 40000.0, 0.2, 1, 2)
+
+
+@pytest.mark.parametrize("change,exc,msg", [
+    (dict(num_hori=3), ValueError, "'num_hori' must be in the range [4, 1440]"),
+    (dict(num_hori=1441), ValueError, "'num_hori' must be in the range [4, 1440]"),
+    (dict(grid_type=2), ValueError, "'grid_type' must be in the range [0, 1]"),
+    (dict(dist_search=999.0), ValueError, "'dist_search' must be in the range [1'000, 500'000] km"),
+    (dict(dist_search=500001.0), ValueError, "'dist_search' must be in the range"),
+    (dict(ray_org_elev=0.05), TypeError, "Minimal allowed value for 'ray_org_elev' is 0.1 m"),
+    (dict(refine_factor=0), ValueError, "'refine_factor' must be in the range [1, 50]"),
+    (dict(refine_factor=51), ValueError, "'refine_factor' must be in the range [1, 50]"),
+    (dict(svf_type=3), ValueError, "'svf_type' must be in the range [0, 2]"),
+])
+def test_argument_checks_match_reference(dom, change, exc, msg):
+    names = ("num_hori", "grid_type", "dist_search", "ray_org_elev", "refine_factor",
+             "svf_type")
+    args = dict(zip(names, ARGS))
+    args.update(change)
+    with pytest.raises(exc, match=re.escape(msg)):
+        horizon_svf_comp_py(*dom.inputs(), *[args[n] for n in names])
+
+
+def test_array_checks_match_reference(dom):
+    c = dom.inputs()
+    with pytest.raises(ValueError, match="Inconsistent lengths of input arrays 'clon'"):
+        horizon_svf_comp_py(c[0][:-1], *c[1:], *ARGS)
+    with pytest.raises(ValueError, match="Inconsistent lengths of input arrays 'vlon'"):
+        horizon_svf_comp_py(*c[:3], c[3][:-1], *c[4:], *ARGS)
+    with pytest.raises(ValueError, match="First dimension of 'cells_of_vertex' must have length 6"):
+        horizon_svf_comp_py(*c[:5], c[5][:5], *ARGS)
+    bad = c[5].copy()
+    bad[0, 0] = dom.ncell
+    with pytest.raises(ValueError, match="Indices of 'cells_of_vertex' out of range"):
+        horizon_svf_comp_py(*c[:5], bad, *ARGS)
+    bad[0, 0] = -1
+    with pytest.raises(ValueError, match="Indices of 'cells_of_vertex' out of range"):
+        horizon_svf_comp_py(*c[:5], bad, *ARGS)
+    with pytest.raises(ValueError, match="Buffer dtype mismatch"):
+        horizon_svf_comp_py(c[0].astype(np.float32), *c[1:], *ARGS)
+    with pytest.raises(ValueError, match="Buffer dtype mismatch"):
+        horizon_svf_comp_py(*c[:5], c[5].astype(np.int64), *ARGS)
+    with pytest.raises(ValueError, match="wrong number of dimensions"):
+        horizon_svf_comp_py(c[0][None, :], *c[1:], *ARGS)
+    with pytest.raises(TypeError, match="incorrect type"):
+        horizon_svf_comp_py(list(c[0]), *c[1:], *ARGS)
+    with pytest.raises(TypeError):
+        horizon_svf_comp_py(*c, 24.5, *ARGS[1:])
+    e = np.empty(0)
+    with pytest.raises(IndexError):
+        horizon_svf_comp_py(e, e, e, *c[3:5], np.full((6, c[3].size), -2, np.int32), *ARGS)
