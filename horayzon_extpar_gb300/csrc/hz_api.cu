@@ -84,6 +84,8 @@ struct Buffers {
   void* order_scratch;
   unsigned* cell_bounds;
   int* work;
+  double2 *azim_cs, *elev_cs;
+  double* sin_lattice;
   // misc
   unsigned long long* counters;  // rays, node visits, triangle tests
   int* err;
@@ -133,6 +135,9 @@ Buffers carve(Carver& c, const Sizes& s) {
   b.order_scratch = c.take<char>(cell_order_scratch_bytes(s.ncell));
   b.cell_bounds = c.take<unsigned>(8);
   b.work = c.take<int>(4);
+  b.azim_cs = c.take<double2>(s.nhori * 50);  // L <= num_hori * max refine_factor
+  b.elev_cs = c.take<double2>(kElevTable);
+  b.sin_lattice = c.take<double>(kSinTable);
   b.counters = c.take<unsigned long long>(4);
   b.err = c.take<int>(4);
   return b;
@@ -378,6 +383,10 @@ int run_pipeline(Engine& E, const Problem& pr, const Buffers& b, cudaStream_t s,
     HZ_CUDA(trace_exact(p, opt.count_work != 0, s));
   } else {
     const int adv = opt.advance_min >= 1 && opt.advance_min <= 32 ? opt.advance_min : 16;
+    HZ_CUDA(trace_tables(b.azim_cs, b.elev_cs, b.sin_lattice, p.L, azim_shift, p.hori_acc, s));
+    p.azim_cs = b.azim_cs;
+    p.elev_cs = b.elev_cs;
+    p.sin_lattice = b.sin_lattice;
     HZ_CUDA(cell_order(b.cell_enu, p.cell_begin, p.cell_count, b.order, b.order_scratch,
                        b.cell_bounds, b.work, s));
     HZ_CUDA(trace_flat(p, b.order, b.work, adv, opt.count_work != 0, s));

@@ -90,7 +90,20 @@ struct TraceParams {
   double* skyview;          // [ncell]
   unsigned long long* counters;  // [0] rays, [1] node visits, [2] triangle tests
   int* err;
+  // Lattice tables of the persistent search (trace_tables):
+  const double2* azim_cs;   // [L] cos, sin of azimuth shift + a * 360 deg / L
+  const double2* elev_cs;   // [kElevTable] cos, sin of m * 0.5 deg, m = kElevMin + i
+  const double* sin_lattice;  // [kSinTable] sin(j * 0.25 deg)
 };
+
+constexpr int kElevMin = -256;
+constexpr int kElevTable = 1280;
+constexpr int kSinTable = 2560;
+
+// Fills the lattice tables of p (device FP64 sin/cos), L = p.L entries of
+// azim_cs; shift is the reference's azimuth shift (cpp:662-668).
+cudaError_t trace_tables(double2* azim_cs, double2* elev_cs, double* sin_lattice, int L,
+                         double shift, double hori_acc, cudaStream_t s);
 // One thread per cell, nested loops as in the reference (simple; kept as the
 // second implementation the flattened kernel is tested against).
 cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s);

@@ -79,11 +79,14 @@ struct StaticBuffers {
   void* order_scratch;
   unsigned* cell_bounds;
   int* work;
+  double2 *azim_cs, *elev_cs;
+  double* sin_lattice;
   unsigned long long* counters;
   int* err;
 };
 
-StaticBuffers lay_out(Layout& L, long long ncell, long long nvert, long long max_tri) {
+StaticBuffers lay_out(Layout& L, long long ncell, long long nvert, long long max_tri,
+                      long long num_azimuths) {
   StaticBuffers b;
   std::memset(&b, 0, sizeof(b));
   const long long max_mv = ncell + nvert;
@@ -117,6 +120,9 @@ StaticBuffers lay_out(Layout& L, long long ncell, long long nvert, long long max
   b.order_scratch = L.take<char>(cell_order_scratch_bytes(ncell));
   b.cell_bounds = L.take<unsigned>(8);
   b.work = L.take<int>(4);
+  b.azim_cs = L.take<double2>(num_azimuths);
+  b.elev_cs = L.take<double2>(kElevTable);
+  b.sin_lattice = L.take<double>(kSinTable);
   b.counters = L.take<unsigned long long>(4);
   b.err = L.take<int>(4);
   return b;
@@ -184,7 +190,8 @@ extern "C" int hz_horizon_svf_device_static(
 
   const long long max_tri = (long long)(grid_type == 0 ? 4 : 6) * num_vertex;
   Layout dry{nullptr};
-  lay_out(dry, num_cell, num_vertex, max_tri);
+  const long long num_azimuths = (long long)num_hori * refine_factor;
+  lay_out(dry, num_cell, num_vertex, max_tri, num_azimuths);
   if (dry.off > kStaticScratchBytes) {
     char buf[320];
     snprintf(buf, sizeof(buf),
@@ -207,7 +214,7 @@ extern "C" int hz_horizon_svf_device_static(
   }
   cudaStream_t s = (cudaStream_t)stream;
   Layout lay{(char*)g_static_addr[dev]};
-  const StaticBuffers b = lay_out(lay, num_cell, num_vertex, max_tri);
+  const StaticBuffers b = lay_out(lay, num_cell, num_vertex, max_tri, num_azimuths);
 
   // Cleared every call: the array keeps the previous call's contents.
   HZ_STATIC_CUDA(cudaMemsetAsync(b.err, 0, 4 * sizeof(int), s), "clearing error word");
@@ -284,6 +291,11 @@ extern "C" int hz_horizon_svf_device_static(
   p.err = b.err;
   HZ_STATIC_CUDA(cell_order(b.cell_enu, 0, num_cell, b.order, b.order_scratch, b.cell_bounds,
                             b.work, s), "cell order");
+  HZ_STATIC_CUDA(trace_tables(b.azim_cs, b.elev_cs, b.sin_lattice, p.L, azim_shift,
+                              p.hori_acc, s), "lattice tables");
+  p.azim_cs = b.azim_cs;
+  p.elev_cs = b.elev_cs;
+  p.sin_lattice = b.sin_lattice;
   HZ_STATIC_CUDA(trace_flat(p, b.order, b.work, 16, false, s), "horizon search");
   HZ_STATIC_CUDA(cudaMemcpyAsync(&err, b.err, sizeof(int), cudaMemcpyDeviceToHost, s),
                  "reading error word");

@@ -58,6 +58,19 @@ __device__ __forceinline__ Ray make_ray(float ox, float oy, float oz, float dx, 
   return r;
 }
 
+// FP64 re-evaluation of the three edge functions when one of them is zero
+// (rare). Kept out of line so that the common path carries no FP64 work.
+__device__ __noinline__ void edge_functions_fp64(float Ax, float Ay, float Bx, float By,
+                                                 float Cx, float Cy, float* U, float* V,
+                                                 float* W) {
+  *U = __double2float_rn(__dsub_rn(__dmul_rn((double)Cx, (double)By),
+                                   __dmul_rn((double)Cy, (double)Bx)));
+  *V = __double2float_rn(__dsub_rn(__dmul_rn((double)Ax, (double)Cy),
+                                   __dmul_rn((double)Ay, (double)Cx)));
+  *W = __double2float_rn(__dsub_rn(__dmul_rn((double)Bx, (double)Ay),
+                                   __dmul_rn((double)By, (double)Ax)));
+}
+
 // Woop, Benthin & Wald 2013; hit iff 0 < t <= tfar. Same operation order as
 // the oracle (hz_occlusion.h), every operation rounded to nearest.
 __device__ __forceinline__ bool tri_hit(const Ray& r, const float4 v0, const float4 v1,
@@ -80,14 +93,7 @@ __device__ __forceinline__ bool tri_hit(const Ray& r, const float4 v0, const flo
   float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
   float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
   float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
-  if (U == 0.f || V == 0.f || W == 0.f) {
-    U = __double2float_rn(__dsub_rn(__dmul_rn((double)Cx, (double)By),
-                                    __dmul_rn((double)Cy, (double)Bx)));
-    V = __double2float_rn(__dsub_rn(__dmul_rn((double)Ax, (double)Cy),
-                                    __dmul_rn((double)Ay, (double)Cx)));
-    W = __double2float_rn(__dsub_rn(__dmul_rn((double)Bx, (double)Ay),
-                                    __dmul_rn((double)By, (double)Ax)));
-  }
+  if (U == 0.f || V == 0.f || W == 0.f) edge_functions_fp64(Ax, Ay, Bx, By, Cx, Cy, &U, &V, &W);
   if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
   const float det = __fadd_rn(__fadd_rn(U, V), W);
   if (det == 0.f) return false;
@@ -288,17 +294,61 @@ constexpr int kFlatBlock = 128;
 
 enum : int { kPhaseFirst = 0, kPhaseUp = 1, kPhaseDown = 2 };
 
+// Visits internal node `ref`: descends into the nearer hit child (pushing the
+// other), or pops. Returns false on stack overflow.
+__device__ __forceinline__ bool visit_node(const Node* __restrict__ nodes, const Ray& r,
+                                           int& ref, int* stack, int& sp) {
+  const Node* nd = nodes + ref;
+  const float4 na = __ldg(&nd->a);
+  const float4 nb = __ldg(&nd->b);
+  const float4 nc = __ldg(&nd->c);
+  const float4 ndd = __ldg(&nd->d);
+  const int c0 = __float_as_int(ndd.x), c1 = __float_as_int(ndd.y);
+  float t0, t1;
+  const bool h0 = box_hit(r, na.x, na.y, na.z, na.w, nc.x, nc.y, t0);
+  const bool h1 = c1 != kEmptyRef && box_hit(r, nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, t1);
+  if (h0 && h1) {
+    if (sp >= kStackDepth) return false;
+    const bool near0 = t0 <= t1;
+    stack[sp++] = near0 ? c1 : c0;
+    ref = near0 ? c0 : c1;
+  } else if (h0) {
+    ref = c0;
+  } else if (h1) {
+    ref = c1;
+  } else {
+    ref = sp > 0 ? stack[--sp] : kEmptyRef;
+  }
+  return true;
+}
+
+// Tests the triangles of leaf `ref`; true on the first hit.
+template <bool kCount>
+__device__ __forceinline__ bool test_leaf(const Tri* __restrict__ tris, const Ray& r, int ref,
+                                          unsigned long long& ntest) {
+  const int s0 = leaf_start(ref), cnt = leaf_count(ref);
+  for (int k = s0; k < s0 + cnt; k++) {
+    if (kCount) ntest++;
+    const float4 v0 = __ldg(&tris[k].v0);
+    const float4 v1 = __ldg(&tris[k].v1);
+    const float4 v2 = __ldg(&tris[k].v2);
+    if (tri_hit(r, v0, v1, v2)) return true;
+  }
+  return false;
+}
+
 template <bool kCount>
 __global__ void __launch_bounds__(kFlatBlock, 8)
     k_trace_flat(TraceParams p, const int* __restrict__ order, int* __restrict__ work,
                  int advance_min) {
-  // 0-2 sphere normal, 3-5 ray direction, 6-8 elevation axis,
-  // 9 elevation, 10 sector sum, 11 SVF sum
-  __shared__ double sv[12][kFlatBlock];
+  // Per-lane FP64 search state: 0-2 sphere normal U, 3-5 north N, 6-8 east E,
+  // 9-11 horizontal direction of the current azimuth, 12 elevation
+  // accumulator, 13 sector sum, 14 SVF sum.
+  __shared__ double sv[15][kFlatBlock];
   const int t = threadIdx.x;
   const double ha = p.hori_acc;
 
-  int cell = -1, a = 0, phase = kPhaseFirst, up = 0;
+  int cell = -1, a = 0, phase = kPhaseFirst, up = 0, m = 0;
   bool need = true, start = true, last_hit = false;
   int ref = kEmptyRef, sp = 0;
   int stack[kStackDepth];
@@ -319,6 +369,7 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
             break;
           }
           cell = order ? order[k] : p.cell_begin + k;
+          // Cell frame, mo_lradtopo_horayzon.cpp:694-720.
           const V3 q{p.cell_enu[3LL * cell], p.cell_enu[3LL * cell + 1],
                      p.cell_enu[3LL * cell + 2]};
           V3 normal{q.x - p.centre.x, q.y - p.centre.y, q.z - p.centre.z};
@@ -327,78 +378,87 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
           const double dp = dot3(v_n, normal);
           V3 north{v_n.x - dp * normal.x, v_n.y - dp * normal.y, v_n.z - dp * normal.z};
           unit3(north);
+          const V3 east = cross3(north, normal);
           ox = (float)(q.x + normal.x * p.ray_org_elev);
           oy = (float)(q.y + normal.y * p.ray_org_elev);
           oz = (float)(q.z + normal.z * p.ray_org_elev);
-          const V3 dir = rotate3(north, normal, p.shift_sin, p.shift_cos);
-          V3 axis = cross3(dir, normal);
-          unit3(axis);
           sv[0][t] = normal.x; sv[1][t] = normal.y; sv[2][t] = normal.z;
-          sv[3][t] = dir.x; sv[4][t] = dir.y; sv[5][t] = dir.z;
-          sv[6][t] = axis.x; sv[7][t] = axis.y; sv[8][t] = axis.z;
-          sv[9][t] = 0.0; sv[10][t] = 0.0; sv[11][t] = 0.0;
+          sv[3][t] = north.x; sv[4][t] = north.y; sv[5][t] = north.z;
+          sv[6][t] = east.x; sv[7][t] = east.y; sv[8][t] = east.z;
+          sv[12][t] = 0.0; sv[13][t] = 0.0; sv[14][t] = 0.0;
           a = 0;
+          m = 0;
           phase = kPhaseFirst;
           start = false;
-          emit = true;
-          break;
-        }
-        // Result of the last ray: continue the bracket or close the azimuth.
-        V3 dir{sv[3][t], sv[4][t], sv[5][t]};
-        double elev = sv[9][t];
-        if (phase == kPhaseFirst) {
-          phase = last_hit ? kPhaseUp : kPhaseDown;
-          up = 0;
-        }
-        const bool step_up = phase == kPhaseUp && last_hit && up < kMaxUpSteps;
-        const bool step_dn = phase == kPhaseDown && !last_hit && elev > p.elev_floor;
-        if (step_up || step_dn) {
-          const V3 axis{sv[6][t], sv[7][t], sv[8][t]};
-          if (step_up) {
-            up++;
-            elev += (2.0 * ha);
-            dir = rotate3(dir, axis, p.elev_sin_2ha, p.elev_cos_2ha);
-          } else {
-            elev -= (2.0 * ha);
-            dir = rotate3(dir, axis, -p.elev_sin_2ha, p.elev_cos_2ha);
+        } else {
+          // Result of the last ray: continue the bracket or close the azimuth.
+          double elev = sv[12][t];
+          if (phase == kPhaseFirst) {
+            phase = last_hit ? kPhaseUp : kPhaseDown;
+            up = 0;
           }
-          sv[3][t] = dir.x; sv[4][t] = dir.y; sv[5][t] = dir.z;
-          sv[9][t] = elev;
-          emit = true;
-          break;
+          const bool step_up = phase == kPhaseUp && last_hit && up < kMaxUpSteps;
+          const bool step_dn = phase == kPhaseDown && !last_hit && elev > p.elev_floor;
+          if (step_up || step_dn) {
+            if (step_up) {
+              up++;
+              m++;
+              elev += (2.0 * ha);
+            } else {
+              m--;
+              elev -= (2.0 * ha);
+            }
+            sv[12][t] = elev;
+            emit = true;
+            break;
+          }
+          // cpp:535/546, then the clip / sector / SVF epilogue of cpp:736-754.
+          double h = phase == kPhaseUp ? elev - ha : elev + ha;
+          const int j = phase == kPhaseUp ? 2 * m - 1 : 2 * m + 1;  // h ~ j * ha
+          if (h < 0.0) h = 0.0;
+          double sector = sv[13][t] + h;
+          if ((a + 1) % p.refine == 0) {
+            p.horizon[(long long)(a / p.refine) * p.ncell + cell] =
+                ((sector / kPi) * 180.0) / (double)p.refine;
+            sector = 0.0;
+          }
+          double s = 0.0;
+          if (h > 0.0) s = (j > 0 && j < kSinTable) ? __ldg(&p.sin_lattice[j]) : sin(h);
+          double svf = sv[14][t];
+          if (p.svf_type == 0) svf += (1.0 - s);
+          else if (p.svf_type == 1) svf += (1.0 - (s * s));
+          else svf += (1.0 - (s * s * s));
+          a++;
+          if (a == p.L) {
+            p.skyview[cell] = svf / (double)p.L;
+            start = true;
+            continue;
+          }
+          sv[13][t] = sector;
+          sv[14][t] = svf;
+          phase = kPhaseFirst;
         }
-        double h = phase == kPhaseUp ? elev - ha : elev + ha;
-        const V3 normal{sv[0][t], sv[1][t], sv[2][t]};
-        dir = rotate3(dir, normal, -p.azim_sin, p.azim_cos);
-        if (h < 0.0) h = 0.0;
-        double sector = sv[10][t] + h;
-        if ((a + 1) % p.refine == 0) {
-          p.horizon[(long long)(a / p.refine) * p.ncell + cell] =
-              ((sector / kPi) * 180.0) / (double)p.refine;
-          sector = 0.0;
-        }
-        const double s = sin(h);
-        double svf = sv[11][t];
-        if (p.svf_type == 0) svf += (1.0 - s);
-        else if (p.svf_type == 1) svf += (1.0 - (s * s));
-        else svf += (1.0 - (s * s * s));
-        a++;
-        if (a == p.L) {
-          p.skyview[cell] = svf / (double)p.L;
-          start = true;
-          continue;
-        }
-        sv[10][t] = sector;
-        sv[11][t] = svf;
-        V3 axis = cross3(dir, normal);
-        unit3(axis);
-        sv[3][t] = dir.x; sv[4][t] = dir.y; sv[5][t] = dir.z;
-        sv[6][t] = axis.x; sv[7][t] = axis.y; sv[8][t] = axis.z;
-        phase = kPhaseFirst;
+        // New azimuth (the elevation carries over, cpp:511): horizontal
+        // direction cos(theta_a) N + sin(theta_a) E.
+        const double2 cs = __ldg(&p.azim_cs[a]);
+        sv[9][t] = cs.x * sv[3][t] + cs.y * sv[6][t];
+        sv[10][t] = cs.x * sv[4][t] + cs.y * sv[7][t];
+        sv[11][t] = cs.x * sv[5][t] + cs.y * sv[8][t];
         emit = true;
       }
       if (!alive) break;
-      r = make_ray(ox, oy, oz, (float)sv[3][t], (float)sv[4][t], (float)sv[5][t], p.tfar);
+      // Direction at lattice elevation m: cos(e_m) h_a + sin(e_m) U.
+      double2 ecs;
+      if (m >= kElevMin && m < kElevMin + kElevTable) {
+        ecs = __ldg(&p.elev_cs[m - kElevMin]);
+      } else {
+        const double e = (double)m * (2.0 * ha);
+        ecs = make_double2(cos(e), sin(e));
+      }
+      const float dx = (float)(ecs.x * sv[9][t] + ecs.y * sv[0][t]);
+      const float dy = (float)(ecs.x * sv[10][t] + ecs.y * sv[1][t]);
+      const float dz = (float)(ecs.x * sv[11][t] + ecs.y * sv[2][t]);
+      r = make_ray(ox, oy, oz, dx, dy, dz, p.tfar);
       ref = p.root;
       sp = 0;
       need = false;
@@ -410,44 +470,13 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
     bool fin = false, hit = false;
     if (ref >= 0) {
       if (kCount) nvis++;
-      const Node* nd = p.nodes + ref;
-      const float4 na = __ldg(&nd->a);
-      const float4 nb = __ldg(&nd->b);
-      const float4 nc = __ldg(&nd->c);
-      const float4 ndd = __ldg(&nd->d);
-      const int c0 = __float_as_int(ndd.x), c1 = __float_as_int(ndd.y);
-      float t0, t1;
-      const bool h0 = box_hit(r, na.x, na.y, na.z, na.w, nc.x, nc.y, t0);
-      const bool h1 = c1 != kEmptyRef && box_hit(r, nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, t1);
-      if (h0 && h1) {
-        if (sp >= kStackDepth) {
-          atomicOr(p.err, kErrStack);
-          fin = true;
-          hit = true;
-        } else {
-          const bool near0 = t0 <= t1;
-          stack[sp++] = near0 ? c1 : c0;
-          ref = near0 ? c0 : c1;
-        }
-      } else if (h0) {
-        ref = c0;
-      } else if (h1) {
-        ref = c1;
-      } else {
-        ref = sp > 0 ? stack[--sp] : kEmptyRef;
+      if (!visit_node(p.nodes, r, ref, stack, sp)) {
+        atomicOr(p.err, kErrStack);
+        fin = true;
+        hit = true;
       }
     } else if (ref != kEmptyRef) {
-      const int s0 = leaf_start(ref), cnt = leaf_count(ref);
-      for (int k = s0; k < s0 + cnt; k++) {
-        if (kCount) ntest++;
-        const float4 v0 = __ldg(&p.tris[k].v0);
-        const float4 v1 = __ldg(&p.tris[k].v1);
-        const float4 v2 = __ldg(&p.tris[k].v2);
-        if (tri_hit(r, v0, v1, v2)) {
-          hit = true;
-          break;
-        }
-      }
+      hit = test_leaf<kCount>(p.tris, r, ref, ntest);
       if (hit) fin = true;
       else ref = sp > 0 ? stack[--sp] : kEmptyRef;
     }
@@ -518,6 +547,24 @@ __global__ void k_cell_keys(const double* __restrict__ cell_enu, int begin, int 
   vals[k] = begin + k;
 }
 
+// Lattice tables: azimuths theta_a = shift + a * 2 pi / L (cpp:653-668),
+// elevations m * 2 * hori_acc (cpp:527, 538) and sin(j * hori_acc) for the
+// SVF of clipped horizons on the lattice.
+__global__ void k_trace_tables(double2* __restrict__ azim_cs, double2* __restrict__ elev_cs,
+                               double* __restrict__ sin_lattice, int L, double shift,
+                               double hori_acc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < L) {
+    const double th = shift + (double)i * ((2.0 * kPi) / (double)L);
+    azim_cs[i] = make_double2(cos(th), sin(th));
+  }
+  if (i < kElevTable) {
+    const double e = (double)(kElevMin + i) * (2.0 * hori_acc);
+    elev_cs[i] = make_double2(cos(e), sin(e));
+  }
+  if (i < kSinTable) sin_lattice[i] = sin((double)i * hori_acc);
+}
+
 __global__ void k_init_cell_bounds(unsigned* b, int* work) {
   b[0] = 0xFFFFFFFFu;
   b[1] = 0xFFFFFFFFu;
@@ -527,6 +574,15 @@ __global__ void k_init_cell_bounds(unsigned* b, int* work) {
 }
 
 }  // namespace
+
+cudaError_t trace_tables(double2* azim_cs, double2* elev_cs, double* sin_lattice, int L,
+                         double shift, double hori_acc, cudaStream_t s) {
+  const int n = L > kSinTable ? L : kSinTable;
+  k_trace_tables<<<grid_for(n, 256), 256, 0, s>>>(azim_cs, elev_cs, sin_lattice, L, shift,
+                                                  hori_acc);
+  note_launches(1);
+  return cudaGetLastError();
+}
 
 size_t cell_order_scratch_bytes(long long n) {
   if (n < 1) n = 1;
@@ -553,25 +609,26 @@ cudaError_t cell_order(const double* cell_enu, int begin, int count, int32_t* or
   return radix_sort_pairs(keys, order, keys_alt, vals_alt, count, 32, sort_scratch, s);
 }
 
-cudaError_t trace_flat(const TraceParams& p, const int32_t* order, int* work,
-                       int advance_min, bool count_work, cudaStream_t s) {
-  if (p.cell_count <= 0) return cudaSuccess;
+template <bool kCount>
+cudaError_t launch_flat(const TraceParams& p, const int32_t* order, int* work,
+                        int advance_min, cudaStream_t s) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (count_work)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_flat<true>, kFlatBlock, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_flat<false>, kFlatBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_flat<kCount>, kFlatBlock, 0);
   long long blocks = (long long)sms * (per_sm > 0 ? per_sm : 1);
   const long long needed = (p.cell_count + kFlatBlock - 1) / kFlatBlock;
   if (blocks > needed) blocks = needed;
-  if (count_work)
-    k_trace_flat<true><<<(unsigned)blocks, kFlatBlock, 0, s>>>(p, order, work, advance_min);
-  else
-    k_trace_flat<false><<<(unsigned)blocks, kFlatBlock, 0, s>>>(p, order, work, advance_min);
+  k_trace_flat<kCount><<<(unsigned)blocks, kFlatBlock, 0, s>>>(p, order, work, advance_min);
   note_launches(1);
   return cudaGetLastError();
+}
+
+cudaError_t trace_flat(const TraceParams& p, const int32_t* order, int* work,
+                       int advance_min, bool count_work, cudaStream_t s) {
+  if (p.cell_count <= 0) return cudaSuccess;
+  return count_work ? launch_flat<true>(p, order, work, advance_min, s)
+                    : launch_flat<false>(p, order, work, advance_min, s);
 }
 
 cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s) {
