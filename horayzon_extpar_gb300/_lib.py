@@ -22,7 +22,19 @@ HZ_OK, HZ_ERR_VALUE, HZ_ERR_TYPE, HZ_ERR_INDEX, HZ_ERR_CUDA, HZ_ERR_INTERNAL = r
 EXPORTED_SYMBOLS = ("hz_default_options", "horizon_svf_comp", "hz_horizon_svf",
                     "hz_horizon_svf_device", "hz_build_mesh", "hz_mesh_enu32",
                     "hz_last_error", "hz_version", "hz_release_workspace",
-                    "hz_horizon_svf_device_static")
+                    "hz_horizon_svf_device_static", "hz_horizon_svf_batch")
+
+
+class Domain(C.Structure):
+    """hz_domain: one regional domain of a batch call."""
+    _fields_ = [("clon", C.c_void_p), ("clat", C.c_void_p), ("hsurf", C.c_void_p),
+                ("vlon", C.c_void_p), ("vlat", C.c_void_p),
+                ("cells_of_vertex", C.c_void_p), ("horizon", C.c_void_p),
+                ("skyview", C.c_void_p), ("num_cell", C.c_int32),
+                ("num_vertex", C.c_int32), ("num_hori", C.c_int32),
+                ("grid_type", C.c_int32), ("dist_search", C.c_double),
+                ("ray_org_elev", C.c_double), ("refine_factor", C.c_int32),
+                ("svf_type", C.c_int32), ("latency_ms", C.c_double)]
 
 
 class Options(C.Structure):
@@ -96,6 +108,9 @@ def load(build_if_missing: bool = True):
                                              C.POINTER(Stats)])
         L.hz_horizon_svf_device_static.restype = C.c_int
         L.hz_horizon_svf_device_static.argtypes = [C.c_void_p] * 8 + common + [C.c_void_p]
+        L.hz_horizon_svf_batch.restype = C.c_int
+        L.hz_horizon_svf_batch.argtypes = [C.POINTER(Domain), C.c_int, C.c_int, C.c_void_p,
+                                           C.POINTER(Options), C.POINTER(Stats)]
         L.hz_build_mesh.restype = C.c_int
         L.hz_build_mesh.argtypes = [_D, _D, _D, _D, _D, _I, C.c_int, C.c_int, C.c_int,
                                     _D, _D, _D, C.c_int, _I, C.c_int,

@@ -1,18 +1,24 @@
 // hz_api.cu -- the C ABI (include/horayzon_gb300.h) and the per-device engine
-// that runs mesh assembly, geodetic frames, LBVH build and horizon search.
+// that runs mesh assembly, geodetic frames, LBVH build and horizon search for
+// one domain or a batch of domains.
 //
-// Pipeline of one call (mo_lradtopo_horayzon.cpp:562-785):
-//   mesh_count -> scan -> [read totals, check indices] -> mesh_emit ->
-//   mesh_ecef -> [read cell ECEF sum] -> frame on the host (glibc, same
-//   expressions as cpp:624-644) -> mesh_enu -> bvh_build -> trace -> counters.
+// Pipeline of one call over n domains (mo_lradtopo_horayzon.cpp:562-785 per
+// domain):
+//   mesh_count + scan for every domain -> [read totals, check indices] ->
+//   mesh_emit + mesh_ecef for every domain -> [read cell ECEF sums] -> ENU
+//   frames on the host (glibc, same expressions as cpp:624-644) -> mesh_enu +
+//   bvh_build + lattice tables + Morton cell order for every domain -> ONE
+//   persistent search launch over all cells of all domains -> counters.
 // Device memory comes from one grow-only arena per device, carved per call.
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
-#include <chrono>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/horayzon_gb300.h"
 #include "hz_internal.h"
@@ -57,12 +63,18 @@ struct Carver {
   }
 };
 
-struct Sizes {
-  long long ncell, nvert, nhori;
-  long long max_tri, max_mv;
-  bool host_io;
+// One domain's problem: arrays (device pointers once staged) and arguments.
+struct Problem {
+  const double *clon, *clat, *hsurf, *vlon, *vlat;
+  const int* cov;
+  double *horizon, *skyview;
+  int ncell, nvert, nhori, grid_type;
+  double dist_search, ray_org_elev;
+  int refine, svf_type;
+  int cell_begin, cell_count;  // traced range
 };
 
+// Device buffers of one domain.
 struct Buffers {
   // host-entry staging of inputs/outputs
   double *clon, *clat, *hsurf, *vlon, *vlat;
@@ -79,48 +91,46 @@ struct Buffers {
   Node* nodes;
   Tri* tris;
   BvhScratch bvh;
-  // cell order of the persistent search
-  int32_t* order;
+  // search
   void* order_scratch;
   unsigned* cell_bounds;
-  int* work;
   double2 *azim_cs, *elev_cs;
   double* sin_lattice;
-  // misc
-  unsigned long long* counters;  // rays, node visits, triangle tests
   int* err;
 };
 
-Buffers carve(Carver& c, const Sizes& s) {
+Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhori,
+                     int grid_type, bool host_io) {
   Buffers b;
   std::memset(&b, 0, sizeof(b));
-  if (s.host_io) {
-    b.clon = c.take<double>(s.ncell);
-    b.clat = c.take<double>(s.ncell);
-    b.hsurf = c.take<double>(s.ncell);
-    b.vlon = c.take<double>(s.nvert);
-    b.vlat = c.take<double>(s.nvert);
-    b.cov = c.take<int>(6 * s.nvert);
-    b.horizon = c.take<double>(s.nhori * s.ncell);
-    b.skyview = c.take<double>(s.ncell);
+  const long long max_tri = (grid_type == 0 ? 4 : 6) * nvert;
+  const long long max_mv = ncell + nvert;
+  if (host_io) {
+    b.clon = c.take<double>(ncell);
+    b.clat = c.take<double>(ncell);
+    b.hsurf = c.take<double>(ncell);
+    b.vlon = c.take<double>(nvert);
+    b.vlat = c.take<double>(nvert);
+    b.cov = c.take<int>(6 * nvert);
+    b.horizon = c.take<double>(nhori * ncell);
+    b.skyview = c.take<double>(ncell);
   }
-  b.packed = c.take<unsigned long long>(s.nvert);
-  b.offsets = c.take<unsigned long long>(s.nvert);
-  b.scan_partials = c.take<unsigned long long>(scan_partials(s.nvert));
+  b.packed = c.take<unsigned long long>(nvert);
+  b.offsets = c.take<unsigned long long>(nvert);
+  b.scan_partials = c.take<unsigned long long>(scan_partials(nvert));
   b.totals = c.take<unsigned long long>(4);
-  b.vot = c.take<int>(3 * s.max_tri);
-  b.add_lon = c.take<double>(s.nvert);
-  b.add_lat = c.take<double>(s.nvert);
-  b.add_h = c.take<double>(s.nvert);
-  b.ecef = c.take<double>(3 * s.max_mv);
-  b.block_sums = c.take<double>(3 * (size_t)ecef_blocks((int)s.max_mv));
+  b.vot = c.take<int>(3 * max_tri);
+  b.add_lon = c.take<double>(nvert);
+  b.add_lat = c.take<double>(nvert);
+  b.add_h = c.take<double>(nvert);
+  b.ecef = c.take<double>(3 * max_mv);
+  b.block_sums = c.take<double>(3 * (size_t)ecef_blocks((int)max_mv));
   b.origin_sum = c.take<double>(4);
-  b.vert32 = c.take<float>(3 * s.max_mv);
-  b.cell_enu = c.take<double>(3 * s.ncell);
-  long long nn = s.max_tri > 1 ? s.max_tri - 1 : 1;
-  b.nodes = c.take<Node>(nn);
-  b.tris = c.take<Tri>(s.max_tri);
-  long long nt = s.max_tri > 0 ? s.max_tri : 1;
+  b.vert32 = c.take<float>(3 * max_mv);
+  b.cell_enu = c.take<double>(3 * ncell);
+  const long long nt = max_tri > 0 ? max_tri : 1;
+  b.nodes = c.take<Node>(nt > 1 ? nt - 1 : 1);
+  b.tris = c.take<Tri>(nt);
   b.bvh.keys = c.take<uint32_t>(nt);
   b.bvh.vals = c.take<int32_t>(nt);
   b.bvh.keys_alt = c.take<uint32_t>(nt);
@@ -131,14 +141,34 @@ Buffers carve(Carver& c, const Sizes& s) {
   b.bvh.counter = c.take<int>(nt);
   b.bvh.bounds = c.take<unsigned>(16);
   b.bvh.sort_scratch = c.take<char>(radix_scratch_u32(nt));
-  b.order = c.take<int32_t>(s.ncell);
-  b.order_scratch = c.take<char>(cell_order_scratch_bytes(s.ncell));
+  b.order_scratch = c.take<char>(cell_order_scratch_bytes(ncell));
   b.cell_bounds = c.take<unsigned>(8);
-  b.work = c.take<int>(4);
-  b.azim_cs = c.take<double2>(s.nhori * 50);  // L <= num_hori * max refine_factor
+  b.azim_cs = c.take<double2>(nhori * 50);  // L <= num_hori * max refine_factor
   b.elev_cs = c.take<double2>(kElevTable);
   b.sin_lattice = c.take<double>(kSinTable);
+  b.err = c.take<int>(4);
+  return b;
+}
+
+// Device buffers shared by the domains of one call.
+struct BatchBuffers {
+  DomainDesc* doms;
+  int32_t* order;                 // all work ids
+  int* work;
+  unsigned long long* counters;   // rays, node visits, triangle tests
+  unsigned long long* done;       // per domain: finished cells, completion time
+  unsigned long long* t0;         // globaltimer at the start of the search
+  int* err;
+};
+
+BatchBuffers carve_batch(Carver& c, int n, long long total_cells) {
+  BatchBuffers b;
+  b.doms = c.take<DomainDesc>(n);
+  b.order = c.take<int32_t>(total_cells);
+  b.work = c.take<int>(4);
   b.counters = c.take<unsigned long long>(4);
+  b.done = c.take<unsigned long long>(2 * (size_t)n);
+  b.t0 = c.take<unsigned long long>(2);
   b.err = c.take<int>(4);
   return b;
 }
@@ -150,14 +180,24 @@ struct Engine {
   size_t cap = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};
-  unsigned long long* pinned = nullptr;  // small readbacks
+  unsigned long long* pinned = nullptr;  // readbacks and descriptor staging
+  size_t pinned_words = 0;
 
   int init(int dev) {
     device = dev;
     HZ_CUDA(cudaSetDevice(dev));
     HZ_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     for (auto& e : ev) HZ_CUDA(cudaEventCreate(&e));
-    HZ_CUDA(cudaMallocHost((void**)&pinned, 64 * sizeof(unsigned long long)));
+    return reserve_pinned(4096);
+  }
+
+  int reserve_pinned(size_t words) {
+    if (words <= pinned_words) return HZ_OK;
+    if (pinned) cudaFreeHost(pinned);
+    pinned = nullptr;
+    pinned_words = 0;
+    HZ_CUDA(cudaMallocHost((void**)&pinned, words * sizeof(unsigned long long)));
+    pinned_words = words;
     return HZ_OK;
   }
 
@@ -266,146 +306,233 @@ Frame make_frame(double xo, double yo, double zo) {
   return f;
 }
 
-struct Problem {
-  const double *clon, *clat, *hsurf, *vlon, *vlat;
-  const int* cov;
-  double *horizon, *skyview;
-  int ncell, nvert, nhori, grid_type;
-  double dist_search, ray_org_elev;
-  int refine, svf_type;
-};
+__global__ void k_stamp(unsigned long long* t) {
+  unsigned long long now;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+  *t = now;
+}
 
 enum class Stop { kMesh, kEnu, kFull };
 
-// Runs the pipeline on device pointers in `pr`. With stop != kFull it ends
-// after the mesh (or ENU) stage and leaves results in `b`.
-int run_pipeline(Engine& E, const Problem& pr, const Buffers& b, cudaStream_t s,
-                 const hz_options& opt, hz_stats* st, Stop stop, int* n_tri_out,
-                 int* n_mv_out) {
-  auto t0 = std::chrono::steady_clock::now();
+struct RunOut {
+  std::vector<int> n_tri, n_mv;
+  std::vector<double> latency_ms;
+};
+
+// Runs the pipeline for n domains whose arrays are device pointers in pr[].
+// With stop != kFull it ends after the mesh (or ENU) stage and leaves the
+// results in b[].
+int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const BatchBuffers& bb,
+              cudaStream_t s, const hz_options& opt, hz_stats* st, Stop stop, RunOut* out) {
   g_launches = 0;
-  HZ_CUDA(cudaMemsetAsync(b.err, 0, 4 * sizeof(int), s));
-  HZ_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(unsigned long long), s));
+  out->n_tri.assign(n, 0);
+  out->n_mv.assign(n, 0);
+  out->latency_ms.assign(n, 0.0);
+  // Pinned layout (64-bit words): 0-63 counters and flags; 64 + [0, n) mesh
+  // totals; 64 + [n, 2n) error words; 64 + [2n, 5n) cell ECEF sums; the
+  // search descriptors from word 64 + 5n + 8.
+  const size_t desc_words = (sizeof(DomainDesc) * (size_t)n + 7) / 8;
+  int rc = E.reserve_pinned(64 + 5 * (size_t)n + 8 + desc_words);
+  if (rc) return rc;
+  unsigned long long* pin = E.pinned;
+  for (int d = 0; d < n; d++) HZ_CUDA(cudaMemsetAsync(b[d].err, 0, 4 * sizeof(int), s));
+  HZ_CUDA(cudaMemsetAsync(bb.err, 0, 4 * sizeof(int), s));
+  HZ_CUDA(cudaMemsetAsync(bb.counters, 0, 4 * sizeof(unsigned long long), s));
+  HZ_CUDA(cudaMemsetAsync(bb.done, 0, 2 * sizeof(unsigned long long) * (size_t)n, s));
   HZ_CUDA(cudaEventRecord(E.ev[0], s));
 
   // ---- mesh (cpp:228-317) ----
-  HZ_CUDA(mesh_count(pr.cov, pr.nvert, pr.ncell, pr.grid_type, b.packed, b.err, s));
-  if (pr.nvert > 0) {
-    HZ_CUDA(scan_exclusive_u64(b.packed, b.offsets, pr.nvert, b.totals, b.scan_partials, s));
-    HZ_CUDA(cudaMemcpyAsync(E.pinned, b.totals, sizeof(unsigned long long),
-                            cudaMemcpyDeviceToHost, s));
-  } else {
-    E.pinned[0] = 0;
+  unsigned long long* pin_tot = pin + 64;
+  unsigned long long* pin_err = pin + 64 + n;
+  for (int d = 0; d < n; d++) {
+    const Problem& P = pr[d];
+    HZ_CUDA(mesh_count(P.cov, P.nvert, P.ncell, P.grid_type, b[d].packed, b[d].err, s));
+    if (P.nvert > 0) {
+      HZ_CUDA(scan_exclusive_u64(b[d].packed, b[d].offsets, P.nvert, b[d].totals,
+                                 b[d].scan_partials, s));
+      HZ_CUDA(cudaMemcpyAsync(pin_tot + d, b[d].totals, sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, s));
+    }
+    HZ_CUDA(cudaMemcpyAsync(pin_err + d, b[d].err, sizeof(int), cudaMemcpyDeviceToHost, s));
   }
-  HZ_CUDA(cudaMemcpyAsync(E.pinned + 1, b.err, sizeof(int), cudaMemcpyDeviceToHost, s));
   HZ_CUDA(cudaStreamSynchronize(s));
-  const int err0 = (int)(E.pinned[1] & 0xFFFFFFFFull);
-  if (err0 & kErrBadIndex) return fail(HZ_ERR_INDEX, "Indices of 'cells_of_vertex' out of range");
-  const unsigned long long tot = E.pinned[0];
-  const int n_tri = (int)(tot & 0xFFFFFFFFull);
-  const int nadd = (int)(tot >> 32);
-  const int nmv = pr.ncell + nadd;
-  *n_tri_out = n_tri;
-  *n_mv_out = nmv;
-  if (opt.verbose) {
-    printf("Build triangle mesh from ICON grid cell circumcenters%s\n",
-           pr.grid_type == 0 ? "\n (non-unique triangulation)"
-                             : " and vertices\n (unique triangulation)");
-    printf("Number of triangles in mesh: %d\n", n_tri);
+  std::vector<int> nadd(n);
+  for (int d = 0; d < n; d++) {
+    if ((int)(pin_err[d] & 0xFFFFFFFFull) & kErrBadIndex)
+      return fail(HZ_ERR_INDEX, "Indices of 'cells_of_vertex' out of range%s",
+                  n > 1 ? " (batch domain)" : "");
+    const unsigned long long tot = pr[d].nvert > 0 ? pin_tot[d] : 0ull;
+    out->n_tri[d] = (int)(tot & 0xFFFFFFFFull);
+    nadd[d] = (int)(tot >> 32);
+    out->n_mv[d] = pr[d].ncell + nadd[d];
+    if (opt.verbose) {
+      printf("Build triangle mesh from ICON grid cell circumcenters%s\n",
+             pr[d].grid_type == 0 ? "\n (non-unique triangulation)"
+                                  : " and vertices\n (unique triangulation)");
+      printf("Number of triangles in mesh: %d\n", out->n_tri[d]);
+    }
   }
-  HZ_CUDA(mesh_emit(pr.clon, pr.clat, pr.hsurf, pr.vlon, pr.vlat, pr.cov, pr.nvert, pr.ncell,
-                    pr.grid_type, b.offsets, b.vot, b.add_lon, b.add_lat, b.add_h, s));
+  for (int d = 0; d < n; d++) {
+    const Problem& P = pr[d];
+    HZ_CUDA(mesh_emit(P.clon, P.clat, P.hsurf, P.vlon, P.vlat, P.cov, P.nvert, P.ncell,
+                      P.grid_type, b[d].offsets, b[d].vot, b[d].add_lon, b[d].add_lat,
+                      b[d].add_h, s));
+  }
   if (stop == Stop::kMesh) return HZ_OK;
 
   // ---- frames (cpp:611-644) ----
-  HZ_CUDA(mesh_ecef(pr.clon, pr.clat, pr.hsurf, b.add_lon, b.add_lat, b.add_h, pr.ncell, nadd,
-                    b.ecef, b.block_sums, b.origin_sum, s));
-  HZ_CUDA(cudaMemcpyAsync(E.pinned + 2, b.origin_sum, 3 * sizeof(double),
-                          cudaMemcpyDeviceToHost, s));
-  HZ_CUDA(cudaStreamSynchronize(s));
-  double so[3];
-  std::memcpy(so, E.pinned + 2, sizeof(so));
-  const Frame fr = make_frame(so[0], so[1], so[2]);
-  if (opt.verbose) {
-    double radius = sqrt(so[0] * so[0] + so[1] * so[1] + so[2] * so[2]);
-    printf("Origin of ENU coordinate system: %.4f deg lat, %.4f deg lon\n",
-           rad2deg(asin(so[2] / radius)), rad2deg(atan2(so[1], so[0])));
+  for (int d = 0; d < n; d++) {
+    const Problem& P = pr[d];
+    HZ_CUDA(mesh_ecef(P.clon, P.clat, P.hsurf, b[d].add_lon, b[d].add_lat, b[d].add_h,
+                      P.ncell, nadd[d], b[d].ecef, b[d].block_sums, b[d].origin_sum, s));
   }
-  HZ_CUDA(mesh_enu(b.ecef, nmv, pr.ncell, fr, b.vert32, b.cell_enu, s));
+  double* sums = reinterpret_cast<double*>(pin + 64 + 2 * n);
+  for (int d = 0; d < n; d++)
+    HZ_CUDA(cudaMemcpyAsync(sums + 3 * d, b[d].origin_sum, 3 * sizeof(double),
+                            cudaMemcpyDeviceToHost, s));
+  HZ_CUDA(cudaStreamSynchronize(s));
+  std::vector<Frame> frames(n);
+  for (int d = 0; d < n; d++) {
+    frames[d] = make_frame(sums[3 * d], sums[3 * d + 1], sums[3 * d + 2]);
+    if (opt.verbose) {
+      const double* so = sums + 3 * d;
+      const double radius = sqrt(so[0] * so[0] + so[1] * so[1] + so[2] * so[2]);
+      printf("Origin of ENU coordinate system: %.4f deg lat, %.4f deg lon\n",
+             rad2deg(asin(so[2] / radius)), rad2deg(atan2(so[1], so[0])));
+    }
+    HZ_CUDA(mesh_enu(b[d].ecef, out->n_mv[d], pr[d].ncell, frames[d], b[d].vert32,
+                     b[d].cell_enu, s));
+  }
   HZ_CUDA(cudaEventRecord(E.ev[1], s));
   if (stop == Stop::kEnu) return HZ_OK;
 
   // ---- BVH (cpp:395-432) ----
-  HZ_CUDA(bvh_build(b.vert32, b.vot, n_tri, b.nodes, b.tris, b.bvh, s));
+  for (int d = 0; d < n; d++)
+    HZ_CUDA(bvh_build(b[d].vert32, b[d].vot, out->n_tri[d], b[d].nodes, b[d].tris, b[d].bvh, s));
   HZ_CUDA(cudaEventRecord(E.ev[2], s));
 
   // ---- horizon + SVF (cpp:651-761) ----
-  TraceParams p;
-  std::memset(&p, 0, sizeof(p));
-  p.cell_enu = b.cell_enu;
-  p.ncell = pr.ncell;
-  p.cell_begin = 0;
-  p.cell_count = pr.ncell;
-  if (opt.cell_count > 0) {
-    if (opt.cell_begin < 0 || (long long)opt.cell_begin + opt.cell_count > pr.ncell)
-      return fail(HZ_ERR_VALUE, "cell range [%d, %d) outside [0, %d)", opt.cell_begin,
-                  opt.cell_begin + opt.cell_count, pr.ncell);
-    p.cell_begin = opt.cell_begin;
-    p.cell_count = opt.cell_count;
+  const double hori_acc = deg2rad(0.25);
+  const double elev_floor = deg2rad(opt.elev_floor_deg);
+  std::vector<double> shift(n);
+  for (int d = 0; d < n; d++) {
+    const int L = pr[d].nhori * pr[d].refine;
+    shift[d] = 0.0;
+    if (pr[d].refine != 1)
+      shift[d] = -(deg2rad(360.0) / (2.0 * pr[d].nhori)) + (deg2rad(360.0) / (2.0 * (double)L));
   }
-  p.nodes = b.nodes;
-  p.tris = b.tris;
-  p.root = n_tri > 0 ? 0 : kEmptyRef;
-  p.centre = fr.centre;
-  p.pole = fr.pole;
-  p.ray_org_elev = pr.ray_org_elev;
-  p.tfar = (float)pr.dist_search;
-  p.nhori = pr.nhori;
-  p.refine = pr.refine;
-  p.L = pr.nhori * pr.refine;
-  p.svf_type = pr.svf_type;
-  p.hori_acc = deg2rad(0.25);
-  p.elev_floor = deg2rad(opt.elev_floor_deg);
-  p.azim_sin = sin(deg2rad(360.0) / (double)p.L);
-  p.azim_cos = cos(deg2rad(360.0) / (double)p.L);
-  p.elev_sin_2ha = sin(2.0 * p.hori_acc);
-  p.elev_cos_2ha = cos(2.0 * p.hori_acc);
-  double azim_shift = 0.0;
-  if (pr.refine != 1)
-    azim_shift = -(deg2rad(360.0) / (2.0 * pr.nhori)) + (deg2rad(360.0) / (2.0 * (double)p.L));
-  p.shift_sin = sin(-azim_shift);
-  p.shift_cos = cos(-azim_shift);
-  p.horizon = pr.horizon;
-  p.skyview = pr.skyview;
-  p.counters = b.counters;
-  p.err = b.err;
-  if (opt.kernel == HZ_KERNEL_PER_CELL) {
+  if (opt.kernel == HZ_KERNEL_PER_CELL && n == 1) {
+    const Problem& P = pr[0];
+    TraceParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.cell_enu = b[0].cell_enu;
+    p.ncell = P.ncell;
+    p.cell_begin = P.cell_begin;
+    p.cell_count = P.cell_count;
+    p.nodes = b[0].nodes;
+    p.tris = b[0].tris;
+    p.root = out->n_tri[0] > 0 ? 0 : kEmptyRef;
+    p.centre = frames[0].centre;
+    p.pole = frames[0].pole;
+    p.ray_org_elev = P.ray_org_elev;
+    p.tfar = (float)P.dist_search;
+    p.nhori = P.nhori;
+    p.refine = P.refine;
+    p.L = P.nhori * P.refine;
+    p.svf_type = P.svf_type;
+    p.hori_acc = hori_acc;
+    p.elev_floor = elev_floor;
+    p.azim_sin = sin(deg2rad(360.0) / (double)p.L);
+    p.azim_cos = cos(deg2rad(360.0) / (double)p.L);
+    p.elev_sin_2ha = sin(2.0 * p.hori_acc);
+    p.elev_cos_2ha = cos(2.0 * p.hori_acc);
+    p.shift_sin = sin(-shift[0]);
+    p.shift_cos = cos(-shift[0]);
+    p.horizon = P.horizon;
+    p.skyview = P.skyview;
+    p.counters = bb.counters;
+    p.err = bb.err;
     HZ_CUDA(trace_exact(p, opt.count_work != 0, s));
   } else {
+    DomainDesc* desc = reinterpret_cast<DomainDesc*>(pin + 64 + 5 * (size_t)n + 8);
+    long long total = 0;
+    for (int d = 0; d < n; d++) {
+      const Problem& P = pr[d];
+      const int L = P.nhori * P.refine;
+      HZ_CUDA(trace_tables(b[d].azim_cs, b[d].elev_cs, b[d].sin_lattice, L, shift[d],
+                           hori_acc, s));
+      HZ_CUDA(cell_order(b[d].cell_enu, P.cell_begin, P.cell_count, (int)(total - P.cell_begin),
+                         bb.order + total, b[d].order_scratch, b[d].cell_bounds, bb.work, s));
+      DomainDesc D;
+      std::memset(&D, 0, sizeof(D));
+      D.cell_enu = b[d].cell_enu;
+      D.nodes = b[d].nodes;
+      D.tris = b[d].tris;
+      D.horizon = P.horizon;
+      D.skyview = P.skyview;
+      D.azim_cs = b[d].azim_cs;
+      D.elev_cs = b[d].elev_cs;
+      D.sin_lattice = b[d].sin_lattice;
+      D.done = n > 1 ? bb.done + 2 * d : nullptr;
+      D.centre = frames[d].centre;
+      D.pole = frames[d].pole;
+      D.ray_org_elev = P.ray_org_elev;
+      D.hori_acc = hori_acc;
+      D.elev_floor = elev_floor;
+      D.cell_offset = total - P.cell_begin;
+      D.root = out->n_tri[d] > 0 ? 0 : kEmptyRef;
+      D.ncell = P.ncell;
+      D.ncell_traced = P.cell_count;
+      D.nhori = P.nhori;
+      D.refine = P.refine;
+      D.L = L;
+      D.svf_type = P.svf_type;
+      D.tfar = (float)P.dist_search;
+      desc[d] = D;
+      total += P.cell_count;
+    }
+    if (total > INT32_MAX) return fail(HZ_ERR_VALUE, "more than 2^31 cells in one call");
+    HZ_CUDA(cudaMemcpyAsync(bb.doms, desc, sizeof(DomainDesc) * (size_t)n,
+                            cudaMemcpyHostToDevice, s));
     const int adv = opt.advance_min >= 1 && opt.advance_min <= 32 ? opt.advance_min : 16;
-    HZ_CUDA(trace_tables(b.azim_cs, b.elev_cs, b.sin_lattice, p.L, azim_shift, p.hori_acc, s));
-    p.azim_cs = b.azim_cs;
-    p.elev_cs = b.elev_cs;
-    p.sin_lattice = b.sin_lattice;
-    HZ_CUDA(cell_order(b.cell_enu, p.cell_begin, p.cell_count, b.order, b.order_scratch,
-                       b.cell_bounds, b.work, s));
-    HZ_CUDA(trace_flat(p, b.order, b.work, adv, opt.count_work != 0, s));
+    k_stamp<<<1, 1, 0, s>>>(bb.t0);
+    note_launches(1);
+    HZ_CUDA(cudaGetLastError());
+    HZ_CUDA(trace_flat(bb.doms, n, bb.order, (int)total, bb.work, bb.counters, bb.err, adv,
+                       opt.count_work != 0, s));
   }
   HZ_CUDA(cudaEventRecord(E.ev[3], s));
 
-  HZ_CUDA(cudaMemcpyAsync(E.pinned + 8, b.counters, 3 * sizeof(unsigned long long),
+  // Counters, error word, and per-domain completion times.
+  unsigned long long* rb = pin;  // words 0..15 (descriptors live beyond word 64)
+  HZ_CUDA(cudaMemcpyAsync(rb + 8, bb.counters, 3 * sizeof(unsigned long long),
                           cudaMemcpyDeviceToHost, s));
-  HZ_CUDA(cudaMemcpyAsync(E.pinned + 12, b.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HZ_CUDA(cudaMemcpyAsync(rb + 12, bb.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HZ_CUDA(cudaMemcpyAsync(rb + 14, bb.t0, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  unsigned long long* rb_done = pin + 64;  // the totals / error slots are no longer needed
+  if (n > 1)
+    HZ_CUDA(cudaMemcpyAsync(rb_done, bb.done, 2 * sizeof(unsigned long long) * (size_t)n,
+                            cudaMemcpyDeviceToHost, s));
   HZ_CUDA(cudaStreamSynchronize(s));
-  const int err1 = (int)(E.pinned[12] & 0xFFFFFFFFull);
+  const int err1 = (int)(rb[12] & 0xFFFFFFFFull);
   if (err1 & kErrStack) return fail(HZ_ERR_INTERNAL, "BVH traversal stack overflow");
+  if (n > 1)
+    for (int d = 0; d < n; d++)
+      out->latency_ms[d] = rb_done[2 * d + 1] > rb[14]
+                               ? (double)(rb_done[2 * d + 1] - rb[14]) * 1e-6
+                               : 0.0;
   if (st) {
     st->kernel_launches = g_launches;
-    st->num_rays = (int64_t)E.pinned[8];
-    st->node_visits = (int64_t)E.pinned[9];
-    st->tri_tests = (int64_t)E.pinned[10];
-    st->n_tri = n_tri;
-    st->n_mesh_vert = nmv;
+    st->num_rays = (int64_t)rb[8];
+    st->node_visits = (int64_t)rb[9];
+    st->tri_tests = (int64_t)rb[10];
+    long long ntri = 0, nmv = 0;
+    for (int d = 0; d < n; d++) {
+      ntri += out->n_tri[d];
+      nmv += out->n_mv[d];
+    }
+    st->n_tri = (int32_t)std::min<long long>(ntri, INT32_MAX);
+    st->n_mesh_vert = (int32_t)std::min<long long>(nmv, INT32_MAX);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, E.ev[0], E.ev[1]);
     st->ms_mesh = ms;
@@ -415,11 +542,16 @@ int run_pipeline(Engine& E, const Problem& pr, const Buffers& b, cudaStream_t s,
     st->ms_trace = ms;
   }
   if (opt.verbose) {
-    printf("Number of rays shot: %lld\n", (long long)E.pinned[8]);
+    long long cells = 0, evals = 0;
+    for (int d = 0; d < n; d++) {
+      cells += pr[d].cell_count;
+      evals += (long long)pr[d].cell_count * pr[d].nhori;
+    }
+    printf("Number of rays shot: %lld\n", (long long)rb[8]);
     printf("Average number of rays per cell and azimuth sector: %.2f\n",
-           (double)E.pinned[8] / ((double)pr.ncell * (double)pr.nhori));
+           (double)rb[8] / (double)(evals > 0 ? evals : 1));
+    (void)cells;
   }
-  (void)t0;
   return HZ_OK;
 }
 
@@ -433,6 +565,172 @@ hz_options resolve(const hz_options* opt) {
     o.size = sizeof(o);
   }
   return o;
+}
+
+int cell_range(const hz_options& opt, int ncell, int* begin, int* count) {
+  *begin = 0;
+  *count = ncell;
+  if (opt.cell_count > 0) {
+    if (opt.cell_begin < 0 || (long long)opt.cell_begin + opt.cell_count > ncell)
+      return fail(HZ_ERR_VALUE, "cell range [%d, %d) outside [0, %d)", opt.cell_begin,
+                  opt.cell_begin + opt.cell_count, ncell);
+    *begin = opt.cell_begin;
+    *count = opt.cell_count;
+  }
+  return HZ_OK;
+}
+
+// Host <-> device staging of one domain for the host entry points.
+int stage_inputs(const hz_domain& h, const Buffers& b, cudaStream_t s) {
+  const size_t nc = (size_t)h.num_cell, nv = (size_t)h.num_vertex;
+  HZ_CUDA(cudaMemcpyAsync(b.clon, h.clon, nc * 8, cudaMemcpyHostToDevice, s));
+  HZ_CUDA(cudaMemcpyAsync(b.clat, h.clat, nc * 8, cudaMemcpyHostToDevice, s));
+  HZ_CUDA(cudaMemcpyAsync(b.hsurf, h.hsurf, nc * 8, cudaMemcpyHostToDevice, s));
+  if (nv) {
+    HZ_CUDA(cudaMemcpyAsync(b.vlon, h.vlon, nv * 8, cudaMemcpyHostToDevice, s));
+    HZ_CUDA(cudaMemcpyAsync(b.vlat, h.vlat, nv * 8, cudaMemcpyHostToDevice, s));
+    HZ_CUDA(cudaMemcpyAsync(b.cov, h.cells_of_vertex, nv * 6 * 4, cudaMemcpyHostToDevice, s));
+  }
+  return HZ_OK;
+}
+
+int unstage_outputs(const hz_domain& h, const Buffers& b, int begin, int count,
+                    cudaStream_t s) {
+  const size_t nc = (size_t)h.num_cell;
+  if (begin != 0 || count != h.num_cell) {
+    // Only the traced columns: the caller's other entries stay untouched.
+    const size_t c0 = (size_t)begin, cn = (size_t)count;
+    HZ_CUDA(cudaMemcpy2DAsync(h.horizon + c0, nc * 8, b.horizon + c0, nc * 8, cn * 8,
+                              (size_t)h.num_hori, cudaMemcpyDeviceToHost, s));
+    HZ_CUDA(cudaMemcpyAsync(h.skyview + c0, b.skyview + c0, cn * 8, cudaMemcpyDeviceToHost, s));
+  } else {
+    HZ_CUDA(cudaMemcpyAsync(h.horizon, b.horizon, (size_t)h.num_hori * nc * 8,
+                            cudaMemcpyDeviceToHost, s));
+    HZ_CUDA(cudaMemcpyAsync(h.skyview, b.skyview, nc * 8, cudaMemcpyDeviceToHost, s));
+  }
+  return HZ_OK;
+}
+
+// Shared implementation of the host / device, single / batch entry points.
+int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
+              const hz_options& opt, hz_stats* stats) {
+  auto t0 = std::chrono::steady_clock::now();
+  if (n < 1) return fail(HZ_ERR_VALUE, "no domains");
+  long long total_cells = 0;
+  for (int d = 0; d < n; d++) {
+    const hz_domain& h = doms[d];
+    int rc = validate(h.num_cell, h.num_vertex, h.num_hori, h.grid_type, h.dist_search,
+                      h.ray_org_elev, h.refine_factor, h.svf_type);
+    if (rc) return rc;
+    if (!h.clon || !h.clat || !h.hsurf || !h.horizon || !h.skyview ||
+        (h.num_vertex > 0 && (!h.vlon || !h.vlat || !h.cells_of_vertex)))
+      return fail(HZ_ERR_VALUE, "null array pointer");
+    total_cells += h.num_cell;
+  }
+  if (n > 1 && opt.cell_count > 0)
+    return fail(HZ_ERR_VALUE, "a cell range applies to single-domain calls only");
+  Engine* E = nullptr;
+  int rc = get_engine(opt.device, &E);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(E->mu);
+  HZ_CUDA(cudaSetDevice(E->device));
+  cudaStream_t s = on_device ? user_stream : E->stream;
+
+  Carver dry(nullptr);
+  for (int d = 0; d < n; d++)
+    carve_domain(dry, doms[d].num_cell, doms[d].num_vertex, doms[d].num_hori,
+                 doms[d].grid_type, !on_device);
+  carve_batch(dry, n, total_cells);
+  rc = E->reserve(dry.off, s);
+  if (rc) return rc;
+  Carver c(E->arena);
+  std::vector<Buffers> b(n);
+  for (int d = 0; d < n; d++)
+    b[d] = carve_domain(c, doms[d].num_cell, doms[d].num_vertex, doms[d].num_hori,
+                        doms[d].grid_type, !on_device);
+  const BatchBuffers bb = carve_batch(c, n, total_cells);
+
+  std::vector<Problem> pr(n);
+  if (!on_device) HZ_CUDA(cudaEventRecord(E->ev[4], s));
+  for (int d = 0; d < n; d++) {
+    const hz_domain& h = doms[d];
+    if (!on_device) {
+      rc = stage_inputs(h, b[d], s);
+      if (rc) return rc;
+    }
+    Problem& P = pr[d];
+    P.clon = on_device ? h.clon : b[d].clon;
+    P.clat = on_device ? h.clat : b[d].clat;
+    P.hsurf = on_device ? h.hsurf : b[d].hsurf;
+    P.vlon = on_device ? h.vlon : b[d].vlon;
+    P.vlat = on_device ? h.vlat : b[d].vlat;
+    P.cov = on_device ? h.cells_of_vertex : b[d].cov;
+    P.horizon = on_device ? h.horizon : b[d].horizon;
+    P.skyview = on_device ? h.skyview : b[d].skyview;
+    P.ncell = h.num_cell;
+    P.nvert = h.num_vertex;
+    P.nhori = h.num_hori;
+    P.grid_type = h.grid_type;
+    P.dist_search = h.dist_search;
+    P.ray_org_elev = h.ray_org_elev;
+    P.refine = h.refine_factor;
+    P.svf_type = h.svf_type;
+    rc = cell_range(opt, h.num_cell, &P.cell_begin, &P.cell_count);
+    if (rc) return rc;
+  }
+  if (!on_device) HZ_CUDA(cudaEventRecord(E->ev[5], s));
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  RunOut out;
+  rc = run_batch(*E, pr.data(), b.data(), n, bb, s, opt, stats, Stop::kFull, &out);
+  if (rc) return rc;
+  for (int d = 0; d < n; d++) doms[d].latency_ms = out.latency_ms[d];
+  if (!on_device) {
+    HZ_CUDA(cudaEventRecord(E->ev[6], s));
+    for (int d = 0; d < n; d++) {
+      rc = unstage_outputs(doms[d], b[d], pr[d].cell_begin, pr[d].cell_count, s);
+      if (rc) return rc;
+    }
+    HZ_CUDA(cudaEventRecord(E->ev[7], s));
+  }
+  HZ_CUDA(cudaStreamSynchronize(s));
+  if (stats) {
+    if (!on_device) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, E->ev[4], E->ev[5]);
+      stats->ms_h2d = ms;
+      cudaEventElapsedTime(&ms, E->ev[6], E->ev[7]);
+      stats->ms_d2h = ms;
+    }
+    stats->ms_total =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return HZ_OK;
+}
+
+hz_domain make_domain(const double* clon, const double* clat, const double* hsurf,
+                      const double* vlon, const double* vlat, const int32_t* cov,
+                      double* horizon, double* skyview, int num_cell, int num_vertex,
+                      int num_hori, int grid_type, double dist_search, double ray_org_elev,
+                      int refine_factor, int svf_type) {
+  hz_domain h;
+  std::memset(&h, 0, sizeof(h));
+  h.clon = clon;
+  h.clat = clat;
+  h.hsurf = hsurf;
+  h.vlon = vlon;
+  h.vlat = vlat;
+  h.cells_of_vertex = cov;
+  h.horizon = horizon;
+  h.skyview = skyview;
+  h.num_cell = num_cell;
+  h.num_vertex = num_vertex;
+  h.num_hori = num_hori;
+  h.grid_type = grid_type;
+  h.dist_search = dist_search;
+  h.ray_org_elev = ray_org_elev;
+  h.refine_factor = refine_factor;
+  h.svf_type = svf_type;
+  return h;
 }
 
 }  // namespace
@@ -479,37 +777,11 @@ int hz_horizon_svf_device(const double* clon, const double* clat, const double* 
                           int svf_type, void* stream, const hz_options* opt_in,
                           hz_stats* stats) {
   g_last_error.clear();
-  auto t0 = std::chrono::steady_clock::now();
-  hz_options opt = resolve(opt_in);
-  int rc = validate(num_cell, num_vertex, num_hori, grid_type, dist_search, ray_org_elev,
-                    refine_factor, svf_type);
-  if (rc) return rc;
-  Engine* E = nullptr;
-  rc = get_engine(opt.device, &E);
-  if (rc) return rc;
-  std::lock_guard<std::mutex> lock(E->mu);
-  HZ_CUDA(cudaSetDevice(E->device));
-  cudaStream_t s = (cudaStream_t)stream;
-  Sizes sz{num_cell, num_vertex, num_hori,
-           (long long)(grid_type == 0 ? 4 : 6) * num_vertex,
-           (long long)num_cell + num_vertex, false};
-  Carver dry(nullptr);
-  carve(dry, sz);
-  rc = E->reserve(dry.off, s);
-  if (rc) return rc;
-  Carver c(E->arena);
-  Buffers b = carve(c, sz);
-  Problem pr{clon, clat, hsurf, vlon, vlat, cells_of_vertex, horizon, skyview,
-             num_cell, num_vertex, num_hori, grid_type, dist_search, ray_org_elev,
-             refine_factor, svf_type};
-  if (stats) std::memset(stats, 0, sizeof(*stats));
-  int ntri = 0, nmv = 0;
-  rc = run_pipeline(*E, pr, b, s, opt, stats, Stop::kFull, &ntri, &nmv);
-  if (rc) return rc;
-  if (stats)
-    stats->ms_total =
-        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-  return HZ_OK;
+  const hz_options opt = resolve(opt_in);
+  hz_domain h = make_domain(clon, clat, hsurf, vlon, vlat, cells_of_vertex, horizon, skyview,
+                            num_cell, num_vertex, num_hori, grid_type, dist_search,
+                            ray_org_elev, refine_factor, svf_type);
+  return run_entry(&h, 1, true, (cudaStream_t)stream, opt, stats);
 }
 
 int hz_horizon_svf(const double* clon, const double* clat, const double* hsurf,
@@ -519,71 +791,19 @@ int hz_horizon_svf(const double* clon, const double* clat, const double* hsurf,
                    int refine_factor, int svf_type, const hz_options* opt_in,
                    hz_stats* stats) {
   g_last_error.clear();
-  auto t0 = std::chrono::steady_clock::now();
-  hz_options opt = resolve(opt_in);
-  int rc = validate(num_cell, num_vertex, num_hori, grid_type, dist_search, ray_org_elev,
-                    refine_factor, svf_type);
-  if (rc) return rc;
-  if (!clon || !clat || !hsurf || !horizon || !skyview ||
-      (num_vertex > 0 && (!vlon || !vlat || !cells_of_vertex)))
-    return fail(HZ_ERR_VALUE, "null array pointer");
-  Engine* E = nullptr;
-  rc = get_engine(opt.device, &E);
-  if (rc) return rc;
-  std::lock_guard<std::mutex> lock(E->mu);
-  HZ_CUDA(cudaSetDevice(E->device));
-  cudaStream_t s = E->stream;
-  Sizes sz{num_cell, num_vertex, num_hori,
-           (long long)(grid_type == 0 ? 4 : 6) * num_vertex,
-           (long long)num_cell + num_vertex, true};
-  Carver dry(nullptr);
-  carve(dry, sz);
-  rc = E->reserve(dry.off, s);
-  if (rc) return rc;
-  Carver c(E->arena);
-  Buffers b = carve(c, sz);
-  const size_t nc = (size_t)num_cell, nv = (size_t)num_vertex;
-  HZ_CUDA(cudaEventRecord(E->ev[4], s));
-  HZ_CUDA(cudaMemcpyAsync(b.clon, clon, nc * 8, cudaMemcpyHostToDevice, s));
-  HZ_CUDA(cudaMemcpyAsync(b.clat, clat, nc * 8, cudaMemcpyHostToDevice, s));
-  HZ_CUDA(cudaMemcpyAsync(b.hsurf, hsurf, nc * 8, cudaMemcpyHostToDevice, s));
-  if (nv) {
-    HZ_CUDA(cudaMemcpyAsync(b.vlon, vlon, nv * 8, cudaMemcpyHostToDevice, s));
-    HZ_CUDA(cudaMemcpyAsync(b.vlat, vlat, nv * 8, cudaMemcpyHostToDevice, s));
-    HZ_CUDA(cudaMemcpyAsync(b.cov, cells_of_vertex, nv * 6 * 4, cudaMemcpyHostToDevice, s));
-  }
-  HZ_CUDA(cudaEventRecord(E->ev[5], s));
-  Problem pr{b.clon, b.clat, b.hsurf, b.vlon, b.vlat, b.cov, b.horizon, b.skyview,
-             num_cell, num_vertex, num_hori, grid_type, dist_search, ray_org_elev,
-             refine_factor, svf_type};
-  if (stats) std::memset(stats, 0, sizeof(*stats));
-  int ntri = 0, nmv = 0;
-  rc = run_pipeline(*E, pr, b, s, opt, stats, Stop::kFull, &ntri, &nmv);
-  if (rc) return rc;
-  HZ_CUDA(cudaEventRecord(E->ev[6], s));
-  if (opt.cell_count > 0) {
-    // Only the traced columns: the caller's other entries stay untouched.
-    const size_t c0 = (size_t)opt.cell_begin, cn = (size_t)opt.cell_count;
-    HZ_CUDA(cudaMemcpy2DAsync(horizon + c0, nc * 8, b.horizon + c0, nc * 8, cn * 8,
-                              (size_t)num_hori, cudaMemcpyDeviceToHost, s));
-    HZ_CUDA(cudaMemcpyAsync(skyview + c0, b.skyview + c0, cn * 8, cudaMemcpyDeviceToHost, s));
-  } else {
-    HZ_CUDA(cudaMemcpyAsync(horizon, b.horizon, (size_t)num_hori * nc * 8,
-                            cudaMemcpyDeviceToHost, s));
-    HZ_CUDA(cudaMemcpyAsync(skyview, b.skyview, nc * 8, cudaMemcpyDeviceToHost, s));
-  }
-  HZ_CUDA(cudaEventRecord(E->ev[7], s));
-  HZ_CUDA(cudaStreamSynchronize(s));
-  if (stats) {
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, E->ev[4], E->ev[5]);
-    stats->ms_h2d = ms;
-    cudaEventElapsedTime(&ms, E->ev[6], E->ev[7]);
-    stats->ms_d2h = ms;
-    stats->ms_total =
-        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-  }
-  return HZ_OK;
+  const hz_options opt = resolve(opt_in);
+  hz_domain h = make_domain(clon, clat, hsurf, vlon, vlat, cells_of_vertex, horizon, skyview,
+                            num_cell, num_vertex, num_hori, grid_type, dist_search,
+                            ray_org_elev, refine_factor, svf_type);
+  return run_entry(&h, 1, false, nullptr, opt, stats);
+}
+
+int hz_horizon_svf_batch(hz_domain* domains, int n_domains, int on_device, void* stream,
+                         const hz_options* opt_in, hz_stats* stats) {
+  g_last_error.clear();
+  if (!domains || n_domains < 1) return fail(HZ_ERR_VALUE, "no domains");
+  const hz_options opt = resolve(opt_in);
+  return run_entry(domains, n_domains, on_device != 0, (cudaStream_t)stream, opt, stats);
 }
 
 void horizon_svf_comp(double* clon, double* clat, double* hsurf, double* vlon, double* vlat,
@@ -621,34 +841,43 @@ static int mesh_host_common(const double* clon, const double* clat, const double
   std::lock_guard<std::mutex> lock(E->mu);
   HZ_CUDA(cudaSetDevice(E->device));
   cudaStream_t s = E->stream;
-  Sizes sz{num_cell, num_vertex, 4, (long long)(grid_type == 0 ? 4 : 6) * num_vertex,
-           (long long)num_cell + num_vertex, true};
   Carver dry(nullptr);
-  carve(dry, sz);
+  carve_domain(dry, num_cell, num_vertex, 4, grid_type, true);
+  carve_batch(dry, 1, num_cell);
   rc = E->reserve(dry.off, s);
   if (rc) return rc;
   Carver c(E->arena);
-  Buffers b = carve(c, sz);
-  const size_t nc = (size_t)num_cell, nv = (size_t)num_vertex;
-  HZ_CUDA(cudaMemcpyAsync(b.clon, clon, nc * 8, cudaMemcpyHostToDevice, s));
-  HZ_CUDA(cudaMemcpyAsync(b.clat, clat, nc * 8, cudaMemcpyHostToDevice, s));
-  HZ_CUDA(cudaMemcpyAsync(b.hsurf, hsurf, nc * 8, cudaMemcpyHostToDevice, s));
-  if (nv) {
-    HZ_CUDA(cudaMemcpyAsync(b.vlon, vlon, nv * 8, cudaMemcpyHostToDevice, s));
-    HZ_CUDA(cudaMemcpyAsync(b.vlat, vlat, nv * 8, cudaMemcpyHostToDevice, s));
-    HZ_CUDA(cudaMemcpyAsync(b.cov, cov, nv * 6 * 4, cudaMemcpyHostToDevice, s));
-  }
-  Problem pr{b.clon, b.clat, b.hsurf, b.vlon, b.vlat, b.cov, b.horizon, b.skyview,
-             num_cell, num_vertex, 4, grid_type, 1e4, 1.0, 1, 0};
+  const Buffers b = carve_domain(c, num_cell, num_vertex, 4, grid_type, true);
+  const BatchBuffers bb = carve_batch(c, 1, num_cell);
+  hz_domain h = make_domain(clon, clat, hsurf, vlon, vlat, cov, nullptr, nullptr, num_cell,
+                            num_vertex, 4, grid_type, 1e4, 1.0, 1, 0);
+  rc = stage_inputs(h, b, s);
+  if (rc) return rc;
+  Problem pr;
+  std::memset(&pr, 0, sizeof(pr));
+  pr.clon = b.clon;
+  pr.clat = b.clat;
+  pr.hsurf = b.hsurf;
+  pr.vlon = b.vlon;
+  pr.vlat = b.vlat;
+  pr.cov = b.cov;
+  pr.ncell = num_cell;
+  pr.nvert = num_vertex;
+  pr.nhori = 4;
+  pr.grid_type = grid_type;
+  pr.refine = 1;
+  pr.cell_count = num_cell;
   hz_options opt;
   hz_default_options(&opt);
-  int ntri = 0, nmv = 0;
-  rc = run_pipeline(*E, pr, b, s, opt, nullptr, want_enu ? Stop::kEnu : Stop::kMesh, &ntri,
-                    &nmv);
+  RunOut out;
+  rc = run_batch(*E, &pr, &b, 1, bb, s, opt, nullptr, want_enu ? Stop::kEnu : Stop::kMesh,
+                 &out);
   if (rc) return rc;
+  const int nmv = out.n_mv[0], ntri = out.n_tri[0];
   if (nmv > cap_vert || ntri > cap_tri)
     return fail(HZ_ERR_VALUE, "output capacity too small (%d vertices, %d triangles)", nmv,
                 ntri);
+  const size_t nc = (size_t)num_cell;
   if (want_enu) {
     HZ_CUDA(cudaMemcpyAsync(enu32, b.vert32, (size_t)nmv * 3 * 4, cudaMemcpyDeviceToHost, s));
   } else {

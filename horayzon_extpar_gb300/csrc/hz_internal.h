@@ -109,11 +109,35 @@ cudaError_t trace_tables(double2* azim_cs, double2* elev_cs, double* sin_lattice
 cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s);
 // Morton order of cells [begin, begin + count) into order[count]; also resets
 // the work counter used by trace_flat.
+// Work ids are id_offset + cell.
 size_t cell_order_scratch_bytes(long long n);
-cudaError_t cell_order(const double* cell_enu, int begin, int count, int32_t* order,
-                       void* scratch, unsigned* bounds, int* work, cudaStream_t s);
-// Persistent flattened search (same rays and results as trace_exact).
-cudaError_t trace_flat(const TraceParams& p, const int32_t* order, int* work,
-                       int advance_min, bool count_work, cudaStream_t s);
+cudaError_t cell_order(const double* cell_enu, int begin, int count, int id_offset,
+                       int32_t* order, void* scratch, unsigned* bounds, int* work,
+                       cudaStream_t s);
+
+// One domain of the persistent search (device-resident array).
+struct DomainDesc {
+  const double* cell_enu;     // [3 * ncell] FP64 ENU of cell centres
+  const Node* nodes;
+  const Tri* tris;
+  double* horizon;            // [nhori * ncell] degrees
+  double* skyview;            // [ncell]
+  const double2* azim_cs;     // lattice tables (trace_tables)
+  const double2* elev_cs;
+  const double* sin_lattice;
+  unsigned long long* done;   // optional: [0] finished cells, [1] globaltimer at the last
+  double3 centre, pole;       // Earth centre / North Pole in ENU
+  double ray_org_elev, hori_acc, elev_floor;
+  long long cell_offset;      // work id of cell 0 of this domain
+  int root, ncell, ncell_traced, nhori, refine, L, svf_type;
+  float tfar;
+};
+
+// Persistent flattened search (same rays and results as trace_exact) over
+// `total` work ids from `order`; a work id is cell_offset + cell of its
+// domain, and `doms` is sorted by cell_offset.
+cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
+                       int* work, unsigned long long* counters, int* err, int advance_min,
+                       bool count_work, cudaStream_t s);
 
 }  // namespace hz

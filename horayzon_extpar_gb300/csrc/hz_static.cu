@@ -81,6 +81,7 @@ struct StaticBuffers {
   int* work;
   double2 *azim_cs, *elev_cs;
   double* sin_lattice;
+  DomainDesc* dom;
   unsigned long long* counters;
   int* err;
 };
@@ -123,6 +124,7 @@ StaticBuffers lay_out(Layout& L, long long ncell, long long nvert, long long max
   b.azim_cs = L.take<double2>(num_azimuths);
   b.elev_cs = L.take<double2>(kElevTable);
   b.sin_lattice = L.take<double>(kSinTable);
+  b.dom = L.take<DomainDesc>(1);
   b.counters = L.take<unsigned long long>(4);
   b.err = L.take<int>(4);
   return b;
@@ -256,47 +258,43 @@ extern "C" int hz_horizon_svf_device_static(
 
   // BVH and search (cpp:395-432, 651-761).
   HZ_STATIC_CUDA(bvh_build(b.vert32, b.vot, n_tri, b.nodes, b.tris, b.bvh, s), "BVH build");
-  TraceParams p;
-  std::memset(&p, 0, sizeof(p));
-  p.cell_enu = b.cell_enu;
-  p.ncell = num_cell;
-  p.cell_begin = 0;
-  p.cell_count = num_cell;
-  p.nodes = b.nodes;
-  p.tris = b.tris;
-  p.root = n_tri > 0 ? 0 : kEmptyRef;
-  p.centre = fr.centre;
-  p.pole = fr.pole;
-  p.ray_org_elev = ray_org_elev;
-  p.tfar = (float)dist_search;
-  p.nhori = num_hori;
-  p.refine = refine_factor;
-  p.L = num_hori * refine_factor;
-  p.svf_type = svf_type;
-  p.hori_acc = deg2rad_s(0.25);
-  p.elev_floor = deg2rad_s(-85.0);
-  p.azim_sin = sin(deg2rad_s(360.0) / (double)p.L);
-  p.azim_cos = cos(deg2rad_s(360.0) / (double)p.L);
-  p.elev_sin_2ha = sin(2.0 * p.hori_acc);
-  p.elev_cos_2ha = cos(2.0 * p.hori_acc);
+  const int L = num_hori * refine_factor;
   double azim_shift = 0.0;
   if (refine_factor != 1)
-    azim_shift = -(deg2rad_s(360.0) / (2.0 * num_hori)) +
-                 (deg2rad_s(360.0) / (2.0 * (double)p.L));
-  p.shift_sin = sin(-azim_shift);
-  p.shift_cos = cos(-azim_shift);
-  p.horizon = horizon;
-  p.skyview = skyview;
-  p.counters = b.counters;
-  p.err = b.err;
-  HZ_STATIC_CUDA(cell_order(b.cell_enu, 0, num_cell, b.order, b.order_scratch, b.cell_bounds,
+    azim_shift = -(deg2rad_s(360.0) / (2.0 * num_hori)) + (deg2rad_s(360.0) / (2.0 * (double)L));
+  DomainDesc D;
+  std::memset(&D, 0, sizeof(D));
+  D.cell_enu = b.cell_enu;
+  D.nodes = b.nodes;
+  D.tris = b.tris;
+  D.horizon = horizon;
+  D.skyview = skyview;
+  D.azim_cs = b.azim_cs;
+  D.elev_cs = b.elev_cs;
+  D.sin_lattice = b.sin_lattice;
+  D.centre = fr.centre;
+  D.pole = fr.pole;
+  D.ray_org_elev = ray_org_elev;
+  D.hori_acc = deg2rad_s(0.25);
+  D.elev_floor = deg2rad_s(-85.0);
+  D.cell_offset = 0;
+  D.root = n_tri > 0 ? 0 : kEmptyRef;
+  D.ncell = num_cell;
+  D.ncell_traced = num_cell;
+  D.nhori = num_hori;
+  D.refine = refine_factor;
+  D.L = L;
+  D.svf_type = svf_type;
+  D.tfar = (float)dist_search;
+  // Pageable source: the copy has finished with `D` when the call returns.
+  HZ_STATIC_CUDA(cudaMemcpyAsync(b.dom, &D, sizeof(D), cudaMemcpyHostToDevice, s),
+                 "search descriptor");
+  HZ_STATIC_CUDA(cell_order(b.cell_enu, 0, num_cell, 0, b.order, b.order_scratch, b.cell_bounds,
                             b.work, s), "cell order");
-  HZ_STATIC_CUDA(trace_tables(b.azim_cs, b.elev_cs, b.sin_lattice, p.L, azim_shift,
-                              p.hori_acc, s), "lattice tables");
-  p.azim_cs = b.azim_cs;
-  p.elev_cs = b.elev_cs;
-  p.sin_lattice = b.sin_lattice;
-  HZ_STATIC_CUDA(trace_flat(p, b.order, b.work, 16, false, s), "horizon search");
+  HZ_STATIC_CUDA(trace_tables(b.azim_cs, b.elev_cs, b.sin_lattice, L, azim_shift, D.hori_acc,
+                              s), "lattice tables");
+  HZ_STATIC_CUDA(trace_flat(b.dom, 1, b.order, num_cell, b.work, b.counters, b.err, 16, false,
+                            s), "horizon search");
   HZ_STATIC_CUDA(cudaMemcpyAsync(&err, b.err, sizeof(int), cudaMemcpyDeviceToHost, s),
                  "reading error word");
   HZ_STATIC_CUDA(cudaStreamSynchronize(s), "horizon search");

@@ -339,19 +339,23 @@ __device__ __forceinline__ bool test_leaf(const Tri* __restrict__ tris, const Ra
 
 template <bool kCount>
 __global__ void __launch_bounds__(kFlatBlock, 8)
-    k_trace_flat(TraceParams p, const int* __restrict__ order, int* __restrict__ work,
-                 int advance_min) {
+    k_trace_flat(const DomainDesc* __restrict__ doms, int ndom, const int* __restrict__ order,
+                 int total, int* __restrict__ work, unsigned long long* __restrict__ counters,
+                 int* __restrict__ err, int advance_min) {
   // Per-lane FP64 search state: 0-2 sphere normal U, 3-5 north N, 6-8 east E,
   // 9-11 horizontal direction of the current azimuth, 12 elevation
   // accumulator, 13 sector sum, 14 SVF sum.
   __shared__ double sv[15][kFlatBlock];
   const int t = threadIdx.x;
-  const double ha = p.hori_acc;
 
-  int cell = -1, a = 0, phase = kPhaseFirst, up = 0, m = 0;
+  int dom = 0, cell = -1, a = 0, phase = kPhaseFirst, up = 0, m = 0;
   bool need = true, start = true, last_hit = false;
   int ref = kEmptyRef, sp = 0;
   int stack[kStackDepth];
+  const Node* nodes = nullptr;
+  const Tri* tris = nullptr;
+  int root = kEmptyRef;
+  float tfar = 0.f;
   float ox = 0.f, oy = 0.f, oz = 0.f;
   Ray r;
   unsigned long long rays = 0, nvis = 0, ntest = 0;
@@ -364,24 +368,37 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
       while (!emit) {
         if (start) {
           const int k = atomicAdd(work, 1);
-          if (k >= p.cell_count) {
+          if (k >= total) {
             alive = false;
             break;
           }
-          cell = order ? order[k] : p.cell_begin + k;
+          const long long g = order[k];
+          int lo = 0, hi = ndom - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (doms[mid].cell_offset <= g) lo = mid;
+            else hi = mid - 1;
+          }
+          dom = lo;
+          const DomainDesc& D = doms[dom];
+          cell = (int)(g - D.cell_offset);
+          nodes = D.nodes;
+          tris = D.tris;
+          root = D.root;
+          tfar = D.tfar;
           // Cell frame, mo_lradtopo_horayzon.cpp:694-720.
-          const V3 q{p.cell_enu[3LL * cell], p.cell_enu[3LL * cell + 1],
-                     p.cell_enu[3LL * cell + 2]};
-          V3 normal{q.x - p.centre.x, q.y - p.centre.y, q.z - p.centre.z};
+          const V3 q{D.cell_enu[3LL * cell], D.cell_enu[3LL * cell + 1],
+                     D.cell_enu[3LL * cell + 2]};
+          V3 normal{q.x - D.centre.x, q.y - D.centre.y, q.z - D.centre.z};
           unit3(normal);
-          const V3 v_n{p.pole.x - q.x, p.pole.y - q.y, p.pole.z - q.z};
+          const V3 v_n{D.pole.x - q.x, D.pole.y - q.y, D.pole.z - q.z};
           const double dp = dot3(v_n, normal);
           V3 north{v_n.x - dp * normal.x, v_n.y - dp * normal.y, v_n.z - dp * normal.z};
           unit3(north);
           const V3 east = cross3(north, normal);
-          ox = (float)(q.x + normal.x * p.ray_org_elev);
-          oy = (float)(q.y + normal.y * p.ray_org_elev);
-          oz = (float)(q.z + normal.z * p.ray_org_elev);
+          ox = (float)(q.x + normal.x * D.ray_org_elev);
+          oy = (float)(q.y + normal.y * D.ray_org_elev);
+          oz = (float)(q.z + normal.z * D.ray_org_elev);
           sv[0][t] = normal.x; sv[1][t] = normal.y; sv[2][t] = normal.z;
           sv[3][t] = north.x; sv[4][t] = north.y; sv[5][t] = north.z;
           sv[6][t] = east.x; sv[7][t] = east.y; sv[8][t] = east.z;
@@ -392,13 +409,15 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
           start = false;
         } else {
           // Result of the last ray: continue the bracket or close the azimuth.
+          const DomainDesc& D = doms[dom];
+          const double ha = D.hori_acc;
           double elev = sv[12][t];
           if (phase == kPhaseFirst) {
             phase = last_hit ? kPhaseUp : kPhaseDown;
             up = 0;
           }
           const bool step_up = phase == kPhaseUp && last_hit && up < kMaxUpSteps;
-          const bool step_dn = phase == kPhaseDown && !last_hit && elev > p.elev_floor;
+          const bool step_dn = phase == kPhaseDown && !last_hit && elev > D.elev_floor;
           if (step_up || step_dn) {
             if (step_up) {
               up++;
@@ -417,20 +436,29 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
           const int j = phase == kPhaseUp ? 2 * m - 1 : 2 * m + 1;  // h ~ j * ha
           if (h < 0.0) h = 0.0;
           double sector = sv[13][t] + h;
-          if ((a + 1) % p.refine == 0) {
-            p.horizon[(long long)(a / p.refine) * p.ncell + cell] =
-                ((sector / kPi) * 180.0) / (double)p.refine;
+          if ((a + 1) % D.refine == 0) {
+            D.horizon[(long long)(a / D.refine) * D.ncell + cell] =
+                ((sector / kPi) * 180.0) / (double)D.refine;
             sector = 0.0;
           }
           double s = 0.0;
-          if (h > 0.0) s = (j > 0 && j < kSinTable) ? __ldg(&p.sin_lattice[j]) : sin(h);
+          if (h > 0.0) s = (j > 0 && j < kSinTable) ? __ldg(&D.sin_lattice[j]) : sin(h);
           double svf = sv[14][t];
-          if (p.svf_type == 0) svf += (1.0 - s);
-          else if (p.svf_type == 1) svf += (1.0 - (s * s));
+          if (D.svf_type == 0) svf += (1.0 - s);
+          else if (D.svf_type == 1) svf += (1.0 - (s * s));
           else svf += (1.0 - (s * s * s));
           a++;
-          if (a == p.L) {
-            p.skyview[cell] = svf / (double)p.L;
+          if (a == D.L) {
+            D.skyview[cell] = svf / (double)D.L;
+            if (D.done) {
+              // Completion time of the domain's last cell (batch latency).
+              const unsigned long long fin_cells = atomicAdd(&D.done[0], 1ull) + 1ull;
+              if (fin_cells == (unsigned long long)D.ncell_traced) {
+                unsigned long long now;
+                asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+                D.done[1] = now;
+              }
+            }
             start = true;
             continue;
           }
@@ -440,7 +468,7 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
         }
         // New azimuth (the elevation carries over, cpp:511): horizontal
         // direction cos(theta_a) N + sin(theta_a) E.
-        const double2 cs = __ldg(&p.azim_cs[a]);
+        const double2 cs = __ldg(&doms[dom].azim_cs[a]);
         sv[9][t] = cs.x * sv[3][t] + cs.y * sv[6][t];
         sv[10][t] = cs.x * sv[4][t] + cs.y * sv[7][t];
         sv[11][t] = cs.x * sv[5][t] + cs.y * sv[8][t];
@@ -450,16 +478,16 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
       // Direction at lattice elevation m: cos(e_m) h_a + sin(e_m) U.
       double2 ecs;
       if (m >= kElevMin && m < kElevMin + kElevTable) {
-        ecs = __ldg(&p.elev_cs[m - kElevMin]);
+        ecs = __ldg(&doms[dom].elev_cs[m - kElevMin]);
       } else {
-        const double e = (double)m * (2.0 * ha);
+        const double e = (double)m * (2.0 * doms[dom].hori_acc);
         ecs = make_double2(cos(e), sin(e));
       }
       const float dx = (float)(ecs.x * sv[9][t] + ecs.y * sv[0][t]);
       const float dy = (float)(ecs.x * sv[10][t] + ecs.y * sv[1][t]);
       const float dz = (float)(ecs.x * sv[11][t] + ecs.y * sv[2][t]);
-      r = make_ray(ox, oy, oz, dx, dy, dz, p.tfar);
-      ref = p.root;
+      r = make_ray(ox, oy, oz, dx, dy, dz, tfar);
+      ref = root;
       sp = 0;
       need = false;
       rays++;
@@ -470,13 +498,13 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
     bool fin = false, hit = false;
     if (ref >= 0) {
       if (kCount) nvis++;
-      if (!visit_node(p.nodes, r, ref, stack, sp)) {
-        atomicOr(p.err, kErrStack);
+      if (!visit_node(nodes, r, ref, stack, sp)) {
+        atomicOr(err, kErrStack);
         fin = true;
         hit = true;
       }
     } else if (ref != kEmptyRef) {
-      hit = test_leaf<kCount>(p.tris, r, ref, ntest);
+      hit = test_leaf<kCount>(tris, r, ref, ntest);
       if (hit) fin = true;
       else ref = sp > 0 ? stack[--sp] : kEmptyRef;
     }
@@ -492,10 +520,10 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
     ntest = warp_sum_u64(ntest);
   }
   if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&p.counters[0], rays);
+    atomicAdd(&counters[0], rays);
     if (kCount) {
-      atomicAdd(&p.counters[1], nvis);
-      atomicAdd(&p.counters[2], ntest);
+      atomicAdd(&counters[1], nvis);
+      atomicAdd(&counters[2], ntest);
     }
   }
 }
@@ -531,8 +559,8 @@ __device__ __forceinline__ uint32_t spread16(uint32_t x) {
 }
 
 __global__ void k_cell_keys(const double* __restrict__ cell_enu, int begin, int count,
-                            const unsigned* __restrict__ bounds, uint32_t* __restrict__ keys,
-                            int32_t* __restrict__ vals) {
+                            int id_offset, const unsigned* __restrict__ bounds,
+                            uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
   const float mnx = ord2f(bounds[0]), mny = ord2f(bounds[1]);
@@ -544,7 +572,7 @@ __global__ void k_cell_keys(const double* __restrict__ cell_enu, int begin, int 
   const uint32_t qx = fx <= 0.f ? 0u : (fx >= 65535.0f ? 65535u : (uint32_t)fx);
   const uint32_t qy = fy <= 0.f ? 0u : (fy >= 65535.0f ? 65535u : (uint32_t)fy);
   keys[k] = spread16(qx) | (spread16(qy) << 1);
-  vals[k] = begin + k;
+  vals[k] = id_offset + begin + k;
 }
 
 // Lattice tables: azimuths theta_a = shift + a * 2 pi / L (cpp:653-668),
@@ -589,8 +617,9 @@ size_t cell_order_scratch_bytes(long long n) {
   return 4 * sizeof(uint32_t) * (size_t)n + radix_scratch_u32(n) + 64 + 5 * 256;
 }
 
-cudaError_t cell_order(const double* cell_enu, int begin, int count, int32_t* order,
-                       void* scratch, unsigned* bounds, int* work, cudaStream_t s) {
+cudaError_t cell_order(const double* cell_enu, int begin, int count, int id_offset,
+                       int32_t* order, void* scratch, unsigned* bounds, int* work,
+                       cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
   char* base = (char*)scratch;
   auto take = [&](size_t bytes) {
@@ -604,31 +633,36 @@ cudaError_t cell_order(const double* cell_enu, int begin, int count, int32_t* or
   void* sort_scratch = take(radix_scratch_u32(count));
   k_init_cell_bounds<<<1, 1, 0, s>>>(bounds, work);
   k_cell_bounds<<<grid_for(count, 256), 256, 0, s>>>(cell_enu, begin, count, bounds);
-  k_cell_keys<<<grid_for(count, 256), 256, 0, s>>>(cell_enu, begin, count, bounds, keys, order);
+  k_cell_keys<<<grid_for(count, 256), 256, 0, s>>>(cell_enu, begin, count, id_offset, bounds,
+                                                   keys, order);
   note_launches(3);
   return radix_sort_pairs(keys, order, keys_alt, vals_alt, count, 32, sort_scratch, s);
 }
 
 template <bool kCount>
-cudaError_t launch_flat(const TraceParams& p, const int32_t* order, int* work,
-                        int advance_min, cudaStream_t s) {
+cudaError_t launch_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
+                        int* work, unsigned long long* counters, int* err, int advance_min,
+                        cudaStream_t s) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_flat<kCount>, kFlatBlock, 0);
   long long blocks = (long long)sms * (per_sm > 0 ? per_sm : 1);
-  const long long needed = (p.cell_count + kFlatBlock - 1) / kFlatBlock;
+  const long long needed = ((long long)total + kFlatBlock - 1) / kFlatBlock;
   if (blocks > needed) blocks = needed;
-  k_trace_flat<kCount><<<(unsigned)blocks, kFlatBlock, 0, s>>>(p, order, work, advance_min);
+  k_trace_flat<kCount><<<(unsigned)blocks, kFlatBlock, 0, s>>>(doms, ndom, order, total, work,
+                                                               counters, err, advance_min);
   note_launches(1);
   return cudaGetLastError();
 }
 
-cudaError_t trace_flat(const TraceParams& p, const int32_t* order, int* work,
-                       int advance_min, bool count_work, cudaStream_t s) {
-  if (p.cell_count <= 0) return cudaSuccess;
-  return count_work ? launch_flat<true>(p, order, work, advance_min, s)
-                    : launch_flat<false>(p, order, work, advance_min, s);
+cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
+                       int* work, unsigned long long* counters, int* err, int advance_min,
+                       bool count_work, cudaStream_t s) {
+  if (total <= 0 || ndom <= 0) return cudaSuccess;
+  return count_work
+             ? launch_flat<true>(doms, ndom, order, total, work, counters, err, advance_min, s)
+             : launch_flat<false>(doms, ndom, order, total, work, counters, err, advance_min, s);
 }
 
 cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s) {

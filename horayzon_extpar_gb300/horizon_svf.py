@@ -227,3 +227,42 @@ def mesh_enu32(clon, clat, hsurf, vlon, vlat, cells_of_vertex, grid_type, device
                                    C.byref(ntri), int(device))
     _lib.check(rc)
     return enu[:nmv.value], vot[:ntri.value]
+
+
+def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_deg=-85.0,
+                           advance_min=0, return_stats=False):
+    """Many independent domains in one call (one persistent search launch).
+
+    ``domains``: sequence of ``(inputs, args)`` with ``inputs`` the six arrays
+    of :func:`horizon_svf_comp_py` and ``args`` its six scalar arguments
+    ``(num_hori, grid_type, dist_search, ray_org_elev, refine_factor,
+    svf_type)``; each domain has its own. Returns a list of ``(horizon,
+    skyview)`` and, with ``return_stats``, the call statistics plus the
+    per-domain completion latency in ms (from the start of the search).
+    """
+    keep, structs, outs = [], [], []
+    for inputs, args in domains:
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in inputs[:5]]
+        cov = np.ascontiguousarray(inputs[5], dtype=np.int32)
+        num_hori, grid_type, dist_search, ray_org_elev, refine, svf = args
+        _check_args(*arrs, cov, int(num_hori), int(grid_type), float(dist_search),
+                    float(ray_org_elev), int(refine), int(svf))
+        h = np.empty((int(num_hori), arrs[0].size))
+        s = np.empty(arrs[0].size)
+        keep += arrs + [cov]
+        outs.append((h, s))
+        structs.append(_lib.Domain(
+            *(a.ctypes.data for a in arrs), cov.ctypes.data, h.ctypes.data, s.ctypes.data,
+            arrs[0].size, arrs[3].size, int(num_hori), int(grid_type), float(dist_search),
+            float(ray_org_elev), int(refine), int(svf), 0.0))
+    arr = (_lib.Domain * len(structs))(*structs)
+    opt = _options(device, count_work, elev_floor_deg, False, None, 0, advance_min)
+    st = _lib.Stats()
+    rc = _lib.load().hz_horizon_svf_batch(arr, len(structs), 0, None, C.byref(opt),
+                                          C.byref(st))
+    _lib.check(rc)
+    if return_stats:
+        stats = st.as_dict()
+        stats["latency_ms"] = [arr[i].latency_ms for i in range(len(structs))]
+        return outs, stats
+    return outs

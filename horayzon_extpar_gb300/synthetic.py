@@ -344,3 +344,33 @@ def make_config(name: str, seed: int = 0, **overrides) -> Domain:
     d = make_domain(seed=seed, **cfg)
     d.meta["config"] = name
     return d
+
+
+def make_batch(n_domains: int = 64, seed: int = 0, min_cells: float = 1e4,
+               max_cells: float = 5e5, scale: float = 1.0):
+    """Uneven batch of independent regional domains.
+
+    Sizes are log-uniform in [min_cells, max_cells] (times ``scale``), grid
+    spacing uniform in 0.5-2.5 km, each domain with its own terrain seed,
+    relief 1000-4500 m and num_hori drawn from {16, 24, 36}. Domain centres
+    are spread over mid-latitudes. Returns a list of (Domain, args) with args
+    = (num_hori, grid_type, dist_search, ray_org_elev, refine_factor, svf_type).
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_domains):
+        target = float(np.exp(rng.uniform(np.log(min_cells), np.log(max_cells)))) * scale
+        edge = float(rng.uniform(0.5, 2.5))
+        box = math.sqrt(target * (math.sqrt(3.0) / 4.0) * edge * edge)
+        relief = float(rng.uniform(1000.0, 4500.0))
+        hmin = float(rng.uniform(0.0, 800.0))
+        kind = ["fbm_peaks", "fbm_ridged", "eroded"][int(rng.integers(3))]
+        d = make_domain(edge_km=edge, box_km=box, kind=kind, hmin=hmin, hmax=hmin + relief,
+                        hurst=float(rng.uniform(0.6, 0.9)), n_features=int(rng.integers(0, 20)),
+                        seed=seed * 1000 + i + 1, lat0_deg=float(rng.uniform(-60, 60)),
+                        lon0_deg=float(rng.uniform(-160, 160)),
+                        face_rotation_deg=float(rng.uniform(0, 120)))
+        nhori = int(rng.choice([16, 24, 36]))
+        d.meta["config"] = "batch"
+        out.append((d, (nhori, 1, 40000.0, 0.2, 1, 2)))
+    return out

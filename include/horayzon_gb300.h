@@ -126,6 +126,35 @@ int hz_horizon_svf_device(const double* clon, const double* clat, const double* 
                           double ray_org_elev, int refine_factor, int svf_type,
                           void* stream, const hz_options* opt, hz_stats* stats);
 
+/* One regional domain of a batch call (same layouts as hz_horizon_svf). */
+typedef struct hz_domain {
+    const double* clon;
+    const double* clat;
+    const double* hsurf;
+    const double* vlon;
+    const double* vlat;
+    const int32_t* cells_of_vertex;
+    double* horizon;
+    double* skyview;
+    int32_t num_cell, num_vertex, num_hori, grid_type;
+    double dist_search, ray_org_elev;
+    int32_t refine_factor, svf_type;
+    double latency_ms;       /* out: completion time of the domain's last cell,
+                                measured from the start of the search launch */
+} hz_domain;
+
+/*
+ * Many independent domains in one call: mesh, frames and BVH per domain
+ * (each BVH in its own slice of one device arena), then ONE persistent
+ * search launch over the cells of all domains. Every domain carries its own
+ * arguments (num_hori, grid_type, ...). on_device = 0: host arrays (copied
+ * in and out); on_device = 1: device arrays, work enqueued on `stream`. No
+ * reference counterpart: the reference computes one domain per call
+ * (mo_lradtopo_horayzon.cpp:562-785).
+ */
+int hz_horizon_svf_batch(hz_domain* domains, int n_domains, int on_device, void* stream,
+                         const hz_options* opt, hz_stats* stats);
+
 /*
  * Triangle-mesh assembly alone (mo_lradtopo_horayzon.cpp:228-317), on the
  * GPU, host buffers: mesh vertex (lon, lat, elevation) for the cells followed

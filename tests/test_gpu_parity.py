@@ -214,3 +214,21 @@ def test_gpu_cell_range(small_domain, kernel):
     np.testing.assert_array_equal(hr[:, b:e], h[:, b:e])
     np.testing.assert_array_equal(sr[b:e], s[b:e])
     assert np.isnan(sr[:b]).all() and np.isnan(sr[e:]).all()
+
+
+def test_gpu_batch_equals_single_calls():
+    """One batch call (one persistent search over all domains) gives each
+    domain the same result as its own call."""
+    from horayzon_extpar_gb300.horizon_svf import horizon_svf_comp_batch
+    batch = synthetic.make_batch(n_domains=5, seed=7, min_cells=300, max_cells=4000)
+    batch[1] = (batch[1][0], (24, 0, 15000.0, 0.5, 3, 1))
+    batch[3] = (batch[3][0], (8, 1, 30000.0, 0.2, 2, 0))
+    outs, st = horizon_svf_comp_batch([(d.inputs(), a) for d, a in batch], return_stats=True)
+    assert len(st["latency_ms"]) == 5 and all(x > 0 for x in st["latency_ms"])
+    rays = 0
+    for (d, a), (h, s) in zip(batch, outs):
+        h1, s1, st1 = horizon_svf_comp_py(*d.inputs(), *a, return_stats=True)
+        np.testing.assert_array_equal(h, h1)
+        np.testing.assert_array_equal(s, s1)
+        rays += st1["num_rays"]
+    assert st["num_rays"] == rays
