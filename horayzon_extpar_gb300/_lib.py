@@ -41,10 +41,12 @@ class Options(C.Structure):
     _fields_ = [("size", C.c_int32), ("device", C.c_int32), ("count_work", C.c_int32),
                 ("verbose", C.c_int32), ("elev_floor_deg", C.c_double),
                 ("cell_begin", C.c_int32), ("cell_count", C.c_int32),
-                ("kernel", C.c_int32), ("advance_min", C.c_int32)]
+                ("kernel", C.c_int32), ("advance_min", C.c_int32),
+                ("precision", C.c_int32)]
 
 
 HZ_KERNEL_PERSISTENT, HZ_KERNEL_PER_CELL = 0, 1
+HZ_PRECISION_REFERENCE, HZ_PRECISION_LOCAL = 0, 1
 
 
 class Stats(C.Structure):

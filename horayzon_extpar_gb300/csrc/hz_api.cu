@@ -86,6 +86,8 @@ struct Buffers {
   double *add_lon, *add_lat, *add_h;
   double *ecef, *block_sums, *origin_sum;
   float* vert32;
+  float* vert_lo;    // precise mode only
+  float4* tri_lo;    // precise mode only
   double* cell_enu;
   // BVH
   Node* nodes;
@@ -100,7 +102,7 @@ struct Buffers {
 };
 
 Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhori,
-                     int grid_type, bool host_io) {
+                     int grid_type, bool host_io, bool precise = false) {
   Buffers b;
   std::memset(&b, 0, sizeof(b));
   const long long max_tri = (grid_type == 0 ? 4 : 6) * nvert;
@@ -131,6 +133,10 @@ Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhor
   const long long nt = max_tri > 0 ? max_tri : 1;
   b.nodes = c.take<Node>(nt > 1 ? nt - 1 : 1);
   b.tris = c.take<Tri>(nt);
+  if (precise) {
+    b.vert_lo = c.take<float>(3 * max_mv);
+    b.tri_lo = c.take<float4>(3 * nt);
+  }
   b.bvh.keys = c.take<uint32_t>(nt);
   b.bvh.vals = c.take<int32_t>(nt);
   b.bvh.keys_alt = c.take<uint32_t>(nt);
@@ -401,14 +407,15 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
              rad2deg(asin(so[2] / radius)), rad2deg(atan2(so[1], so[0])));
     }
     HZ_CUDA(mesh_enu(b[d].ecef, out->n_mv[d], pr[d].ncell, frames[d], b[d].vert32,
-                     b[d].cell_enu, s));
+                     b[d].cell_enu, b[d].vert_lo, s));
   }
   HZ_CUDA(cudaEventRecord(E.ev[1], s));
   if (stop == Stop::kEnu) return HZ_OK;
 
   // ---- BVH (cpp:395-432) ----
   for (int d = 0; d < n; d++)
-    HZ_CUDA(bvh_build(b[d].vert32, b[d].vot, out->n_tri[d], b[d].nodes, b[d].tris, b[d].bvh, s));
+    HZ_CUDA(bvh_build(b[d].vert32, b[d].vot, out->n_tri[d], b[d].nodes, b[d].tris, b[d].bvh, s,
+                      b[d].vert_lo, b[d].tri_lo));
   HZ_CUDA(cudaEventRecord(E.ev[2], s));
 
   // ---- horizon + SVF (cpp:651-761) ----
@@ -468,6 +475,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.cell_enu = b[d].cell_enu;
       D.nodes = b[d].nodes;
       D.tris = b[d].tris;
+      D.tri_lo = b[d].tri_lo;
       D.horizon = P.horizon;
       D.skyview = P.skyview;
       D.azim_cs = b[d].azim_cs;
@@ -499,7 +507,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     note_launches(1);
     HZ_CUDA(cudaGetLastError());
     HZ_CUDA(trace_flat(bb.doms, n, bb.order, (int)total, bb.work, bb.counters, bb.err, adv,
-                       opt.count_work != 0, s));
+                       opt.count_work != 0, b[0].tri_lo != nullptr, s));
   }
   HZ_CUDA(cudaEventRecord(E.ev[3], s));
 
@@ -636,10 +644,13 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
   HZ_CUDA(cudaSetDevice(E->device));
   cudaStream_t s = on_device ? user_stream : E->stream;
 
+  const bool precise = opt.precision == HZ_PRECISION_LOCAL;
+  if (precise && opt.kernel == HZ_KERNEL_PER_CELL)
+    return fail(HZ_ERR_VALUE, "HZ_PRECISION_LOCAL needs the persistent kernel");
   Carver dry(nullptr);
   for (int d = 0; d < n; d++)
     carve_domain(dry, doms[d].num_cell, doms[d].num_vertex, doms[d].num_hori,
-                 doms[d].grid_type, !on_device);
+                 doms[d].grid_type, !on_device, precise);
   carve_batch(dry, n, total_cells);
   rc = E->reserve(dry.off, s);
   if (rc) return rc;
@@ -647,7 +658,7 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
   std::vector<Buffers> b(n);
   for (int d = 0; d < n; d++)
     b[d] = carve_domain(c, doms[d].num_cell, doms[d].num_vertex, doms[d].num_hori,
-                        doms[d].grid_type, !on_device);
+                        doms[d].grid_type, !on_device, precise);
   const BatchBuffers bb = carve_batch(c, n, total_cells);
 
   std::vector<Problem> pr(n);

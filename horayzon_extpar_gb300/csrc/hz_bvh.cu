@@ -136,18 +136,28 @@ __global__ void k_karras(const uint32_t* __restrict__ keys, int n, Node* __restr
 }
 
 __global__ void k_gather(const float* __restrict__ vert, const int* __restrict__ vot,
-                         const int32_t* __restrict__ order, int n, Tri* __restrict__ tris) {
+                         const int32_t* __restrict__ order, int n, Tri* __restrict__ tris,
+                         const float* __restrict__ vert_lo, float4* __restrict__ tri_lo) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const int t = order[s];
-  const float3 a = load_vert(vert, vot[3LL * t]);
-  const float3 b = load_vert(vert, vot[3LL * t + 1]);
-  const float3 c = load_vert(vert, vot[3LL * t + 2]);
+  const int i0 = vot[3LL * t], i1 = vot[3LL * t + 1], i2 = vot[3LL * t + 2];
+  const float3 a = load_vert(vert, i0);
+  const float3 b = load_vert(vert, i1);
+  const float3 c = load_vert(vert, i2);
   Tri r;
   r.v0 = make_float4(a.x, a.y, a.z, __int_as_float(t));
   r.v1 = make_float4(b.x, b.y, b.z, 0.f);
   r.v2 = make_float4(c.x, c.y, c.z, 0.f);
   tris[s] = r;
+  if (tri_lo) {
+    const float3 la = load_vert(vert_lo, i0);
+    const float3 lb = load_vert(vert_lo, i1);
+    const float3 lc = load_vert(vert_lo, i2);
+    tri_lo[3LL * s + 0] = make_float4(la.x, la.y, la.z, 0.f);
+    tri_lo[3LL * s + 1] = make_float4(lb.x, lb.y, lb.z, 0.f);
+    tri_lo[3LL * s + 2] = make_float4(lc.x, lc.y, lc.z, 0.f);
+  }
 }
 
 struct Box {
@@ -246,7 +256,8 @@ size_t bvh_scratch_bytes(long long n) {
 }
 
 cudaError_t bvh_build(const float* vert32, const int* vot, int n, Node* nodes, Tri* tris,
-                      const BvhScratch& sc, cudaStream_t s) {
+                      const BvhScratch& sc, cudaStream_t s, const float* vert_lo,
+                      float4* tri_lo) {
   if (n <= 0) return cudaSuccess;
   k_init_bounds<<<1, 1, 0, s>>>(sc.bounds);
   k_tri_bounds<<<grid_for(n, 256), 256, 0, s>>>(vert32, vot, n, sc.cxy, sc.bounds);
@@ -255,7 +266,8 @@ cudaError_t bvh_build(const float* vert32, const int* vot, int n, Node* nodes, T
   cudaError_t e = radix_sort_pairs(sc.keys, sc.vals, sc.keys_alt, sc.vals_alt, n, 32,
                                    sc.sort_scratch, s);
   if (e != cudaSuccess) return e;
-  k_gather<<<grid_for(n, 256), 256, 0, s>>>(vert32, vot, sc.vals, n, tris);
+  k_gather<<<grid_for(n, 256), 256, 0, s>>>(vert32, vot, sc.vals, n, tris, vert_lo,
+                                            vert_lo ? tri_lo : nullptr);
   if (n <= kLeafMax) {
     k_small_root<<<1, 1, 0, s>>>(nodes, tris, n, sc.bounds);
     note_launches(2);

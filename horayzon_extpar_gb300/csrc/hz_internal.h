@@ -50,8 +50,9 @@ cudaError_t mesh_ecef(const double* clon, const double* clat, const double* hsur
                       int ncell, int nadd, double* ecef, double* block_sums,
                       double* d_origin_sum, cudaStream_t s);
 // cpp:178-201: FP32 ENU of every mesh vertex, FP64 ENU of every cell.
+// vert_lo (optional, 3 per mesh vertex): FP64 value minus its FP32 rounding.
 cudaError_t mesh_enu(const double* ecef, int nmv, int ncell, const Frame& f,
-                     float* vert32, double* cell_enu, cudaStream_t s);
+                     float* vert32, double* cell_enu, float* vert_lo, cudaStream_t s);
 
 // ---- hz_bvh.cu --------------------------------------------------------------
 struct BvhScratch {
@@ -69,8 +70,11 @@ struct BvhScratch {
 size_t bvh_scratch_bytes(long long n_tri);
 // Builds nodes[n_tri - 1] (or one node when n_tri <= kLeafMax) and tris[n_tri];
 // the root is node 0. n_tri == 0 leaves the tree empty.
+// With vert_lo, also writes tri_lo[3 * n_tri]: the FP32 residuals of v0, v1,
+// v2 per triangle in leaf order (precise mode).
 cudaError_t bvh_build(const float* vert32, const int* vot, int n_tri, Node* nodes,
-                      Tri* tris, const BvhScratch& sc, cudaStream_t s);
+                      Tri* tris, const BvhScratch& sc, cudaStream_t s,
+                      const float* vert_lo = nullptr, float4* tri_lo = nullptr);
 
 // ---- hz_trace.cu ------------------------------------------------------------
 struct TraceParams {
@@ -120,6 +124,7 @@ struct DomainDesc {
   const double* cell_enu;     // [3 * ncell] FP64 ENU of cell centres
   const Node* nodes;
   const Tri* tris;
+  const float4* tri_lo;       // precise mode: [3 * n_tri] FP32 vertex residuals
   double* horizon;            // [nhori * ncell] degrees
   double* skyview;            // [ncell]
   const double2* azim_cs;     // lattice tables (trace_tables)
@@ -136,8 +141,9 @@ struct DomainDesc {
 // Persistent flattened search (same rays and results as trace_exact) over
 // `total` work ids from `order`; a work id is cell_offset + cell of its
 // domain, and `doms` is sorted by cell_offset.
+// precise: every domain carries tri_lo and rays use hi + lo vertices/origin.
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
                        int* work, unsigned long long* counters, int* err, int advance_min,
-                       bool count_work, cudaStream_t s);
+                       bool count_work, bool precise, cudaStream_t s);
 
 }  // namespace hz

@@ -187,7 +187,8 @@ __global__ void k_sum_blocks(const double* __restrict__ block_sums, int nb,
 }
 
 __global__ void k_mesh_enu(const double* __restrict__ ecef, int nmv, int ncell, Frame f,
-                           float* __restrict__ vert32, double* __restrict__ cell_enu) {
+                           float* __restrict__ vert32, double* __restrict__ cell_enu,
+                           float* __restrict__ vert_lo) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nmv) return;
   const double dx = ecef[3LL * i + 0] - f.xe;
@@ -197,9 +198,16 @@ __global__ void k_mesh_enu(const double* __restrict__ ecef, int nmv, int ncell, 
   const double xn = (-f.sin_lon) * dx + f.cos_lon * dy;
   const double yn = f.cyx * dx - f.cyy * dy + f.cos_lat * dz;
   const double zn = f.czx * dx + f.czy * dy + f.sin_lat * dz;
-  vert32[3LL * i + 0] = (float)xn;
-  vert32[3LL * i + 1] = (float)yn;
-  vert32[3LL * i + 2] = (float)zn;
+  const float hx = (float)xn, hy = (float)yn, hz = (float)zn;
+  vert32[3LL * i + 0] = hx;
+  vert32[3LL * i + 1] = hy;
+  vert32[3LL * i + 2] = hz;
+  if (vert_lo) {
+    // Residual of the FP32 rounding: hi + lo carries ~48 bits of the FP64 value.
+    vert_lo[3LL * i + 0] = (float)(xn - (double)hx);
+    vert_lo[3LL * i + 1] = (float)(yn - (double)hy);
+    vert_lo[3LL * i + 2] = (float)(zn - (double)hz);
+  }
   if (i < ncell) {
     cell_enu[3LL * i + 0] = xn;
     cell_enu[3LL * i + 1] = yn;
@@ -245,9 +253,10 @@ cudaError_t mesh_ecef(const double* clon, const double* clat, const double* hsur
 }
 
 cudaError_t mesh_enu(const double* ecef, int nmv, int ncell, const Frame& f, float* vert32,
-                     double* cell_enu, cudaStream_t s) {
+                     double* cell_enu, float* vert_lo, cudaStream_t s) {
   if (nmv <= 0) return cudaSuccess;
-  k_mesh_enu<<<grid_for(nmv, 256), 256, 0, s>>>(ecef, nmv, ncell, f, vert32, cell_enu);
+  k_mesh_enu<<<grid_for(nmv, 256), 256, 0, s>>>(ecef, nmv, ncell, f, vert32, cell_enu,
+                                                vert_lo);
   note_launches(1);
   return cudaGetLastError();
 }

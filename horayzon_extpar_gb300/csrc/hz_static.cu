@@ -254,7 +254,7 @@ extern "C" int hz_horizon_svf_device_static(
                  "reading the ECEF sum");
   HZ_STATIC_CUDA(cudaStreamSynchronize(s), "ECEF");
   const Frame fr = frame_from_sum(sum[0], sum[1], sum[2]);
-  HZ_STATIC_CUDA(mesh_enu(b.ecef, nmv, num_cell, fr, b.vert32, b.cell_enu, s), "ENU");
+  HZ_STATIC_CUDA(mesh_enu(b.ecef, nmv, num_cell, fr, b.vert32, b.cell_enu, nullptr, s), "ENU");
 
   // BVH and search (cpp:395-432, 651-761).
   HZ_STATIC_CUDA(bvh_build(b.vert32, b.vot, n_tri, b.nodes, b.tris, b.bvh, s), "BVH build");
@@ -294,6 +294,7 @@ extern "C" int hz_horizon_svf_device_static(
   HZ_STATIC_CUDA(trace_tables(b.azim_cs, b.elev_cs, b.sin_lattice, L, azim_shift, D.hori_acc,
                               s), "lattice tables");
   HZ_STATIC_CUDA(trace_flat(b.dom, 1, b.order, num_cell, b.work, b.counters, b.err, 16, false,
+                            false,
                             s), "horizon search");
   HZ_STATIC_CUDA(cudaMemcpyAsync(&err, b.err, sizeof(int), cudaMemcpyDeviceToHost, s),
                  "reading error word");

@@ -26,6 +26,7 @@ struct Ray {
   float ix, iy, iz;       // 1 / direction (IEEE)
   float oix, oiy, oiz;    // origin * inverse direction (slab test)
   float pox, poy, poz;    // origin permuted to (kx, ky, kz)
+  float plx, ply, plz;    // precise mode: FP32 residual of the origin, permuted
   float Sx, Sy, Sz;       // shear constants
   int kx, ky, kz;
   float tfar;
@@ -36,7 +37,8 @@ __device__ __forceinline__ float sel3(float x, float y, float z, int k) {
 }
 
 __device__ __forceinline__ Ray make_ray(float ox, float oy, float oz, float dx, float dy,
-                                        float dz, float tfar) {
+                                        float dz, float tfar, float lx = 0.f, float ly = 0.f,
+                                        float lz = 0.f) {
   Ray r;
   r.ox = ox; r.oy = oy; r.oz = oz;
   r.ix = __frcp_rn(dx); r.iy = __frcp_rn(dy); r.iz = __frcp_rn(dz);
@@ -54,6 +56,9 @@ __device__ __forceinline__ Ray make_ray(float ox, float oy, float oz, float dx, 
   r.pox = sel3(ox, oy, oz, kx);
   r.poy = sel3(ox, oy, oz, ky);
   r.poz = sel3(ox, oy, oz, kz);
+  r.plx = sel3(lx, ly, lz, kx);
+  r.ply = sel3(lx, ly, lz, ky);
+  r.plz = sel3(lx, ly, lz, kz);
   r.tfar = tfar;
   return r;
 }
@@ -71,19 +76,12 @@ __device__ __noinline__ void edge_functions_fp64(float Ax, float Ay, float Bx, f
                                    __dmul_rn((double)By, (double)Ax)));
 }
 
-// Woop, Benthin & Wald 2013; hit iff 0 < t <= tfar. Same operation order as
+// Woop, Benthin & Wald 2013 on origin-relative vertices A, B, C given in the
+// ray's (kx, ky, kz) order; hit iff 0 < t <= tfar. Same operation order as
 // the oracle (hz_occlusion.h), every operation rounded to nearest.
-__device__ __forceinline__ bool tri_hit(const Ray& r, const float4 v0, const float4 v1,
-                                        const float4 v2) {
-  const float Akx = __fsub_rn(sel3(v0.x, v0.y, v0.z, r.kx), r.pox);
-  const float Aky = __fsub_rn(sel3(v0.x, v0.y, v0.z, r.ky), r.poy);
-  const float Akz = __fsub_rn(sel3(v0.x, v0.y, v0.z, r.kz), r.poz);
-  const float Bkx = __fsub_rn(sel3(v1.x, v1.y, v1.z, r.kx), r.pox);
-  const float Bky = __fsub_rn(sel3(v1.x, v1.y, v1.z, r.ky), r.poy);
-  const float Bkz = __fsub_rn(sel3(v1.x, v1.y, v1.z, r.kz), r.poz);
-  const float Ckx = __fsub_rn(sel3(v2.x, v2.y, v2.z, r.kx), r.pox);
-  const float Cky = __fsub_rn(sel3(v2.x, v2.y, v2.z, r.ky), r.poy);
-  const float Ckz = __fsub_rn(sel3(v2.x, v2.y, v2.z, r.kz), r.poz);
+__device__ __forceinline__ bool tri_hit_rel(const Ray& r, float Akx, float Aky, float Akz,
+                                            float Bkx, float Bky, float Bkz, float Ckx,
+                                            float Cky, float Ckz) {
   const float Ax = __fsub_rn(Akx, __fmul_rn(r.Sx, Akz));
   const float Ay = __fsub_rn(Aky, __fmul_rn(r.Sy, Akz));
   const float Bx = __fsub_rn(Bkx, __fmul_rn(r.Sx, Bkz));
@@ -104,6 +102,43 @@ __device__ __forceinline__ bool tri_hit(const Ray& r, const float4 v0, const flo
   const float tmax = __fmul_rn(r.tfar, det);
   if (det > 0.f) return T > 0.f && T <= tmax;
   return T < 0.f && T >= tmax;
+}
+
+// Reference arithmetic: FP32 vertices minus the FP32 origin in the domain's
+// global ENU frame (mo_lradtopo_horayzon.cpp:403-410, 715-720).
+__device__ __forceinline__ bool tri_hit(const Ray& r, const float4 v0, const float4 v1,
+                                        const float4 v2) {
+  return tri_hit_rel(r, __fsub_rn(sel3(v0.x, v0.y, v0.z, r.kx), r.pox),
+                     __fsub_rn(sel3(v0.x, v0.y, v0.z, r.ky), r.poy),
+                     __fsub_rn(sel3(v0.x, v0.y, v0.z, r.kz), r.poz),
+                     __fsub_rn(sel3(v1.x, v1.y, v1.z, r.kx), r.pox),
+                     __fsub_rn(sel3(v1.x, v1.y, v1.z, r.ky), r.poy),
+                     __fsub_rn(sel3(v1.x, v1.y, v1.z, r.kz), r.poz),
+                     __fsub_rn(sel3(v2.x, v2.y, v2.z, r.kx), r.pox),
+                     __fsub_rn(sel3(v2.x, v2.y, v2.z, r.ky), r.poy),
+                     __fsub_rn(sel3(v2.x, v2.y, v2.z, r.kz), r.poz));
+}
+
+// Precise arithmetic: vertices and origin as FP32 hi + lo pairs (~48-bit
+// FP64 values); the origin-relative vector (hi - o_hi) + (lo - o_lo) is
+// accurate to FP32 relative to its own length, i.e. centimetres become
+// micrometres for the triangles next to the cell.
+__device__ __forceinline__ float rel(float vh, float vl, float oh, float ol) {
+  return __fadd_rn(__fsub_rn(vh, oh), __fsub_rn(vl, ol));
+}
+__device__ __forceinline__ bool tri_hit_hl(const Ray& r, const float4 v0, const float4 v1,
+                                           const float4 v2, const float4 l0, const float4 l1,
+                                           const float4 l2) {
+  return tri_hit_rel(
+      r, rel(sel3(v0.x, v0.y, v0.z, r.kx), sel3(l0.x, l0.y, l0.z, r.kx), r.pox, r.plx),
+      rel(sel3(v0.x, v0.y, v0.z, r.ky), sel3(l0.x, l0.y, l0.z, r.ky), r.poy, r.ply),
+      rel(sel3(v0.x, v0.y, v0.z, r.kz), sel3(l0.x, l0.y, l0.z, r.kz), r.poz, r.plz),
+      rel(sel3(v1.x, v1.y, v1.z, r.kx), sel3(l1.x, l1.y, l1.z, r.kx), r.pox, r.plx),
+      rel(sel3(v1.x, v1.y, v1.z, r.ky), sel3(l1.x, l1.y, l1.z, r.ky), r.poy, r.ply),
+      rel(sel3(v1.x, v1.y, v1.z, r.kz), sel3(l1.x, l1.y, l1.z, r.kz), r.poz, r.plz),
+      rel(sel3(v2.x, v2.y, v2.z, r.kx), sel3(l2.x, l2.y, l2.z, r.kx), r.pox, r.plx),
+      rel(sel3(v2.x, v2.y, v2.z, r.ky), sel3(l2.x, l2.y, l2.z, r.ky), r.poy, r.ply),
+      rel(sel3(v2.x, v2.y, v2.z, r.kz), sel3(l2.x, l2.y, l2.z, r.kz), r.poz, r.plz));
 }
 
 // Conservative slab test: the boxes carry a margin far above the rounding of
@@ -322,22 +357,31 @@ __device__ __forceinline__ bool visit_node(const Node* __restrict__ nodes, const
   return true;
 }
 
-// Tests the triangles of leaf `ref`; true on the first hit.
-template <bool kCount>
-__device__ __forceinline__ bool test_leaf(const Tri* __restrict__ tris, const Ray& r, int ref,
-                                          unsigned long long& ntest) {
+// Tests the triangles of leaf `ref`; true on the first hit. kPrecise: with
+// the FP32 residuals in tri_lo (hi + lo vertices, hi + lo origin).
+template <bool kCount, bool kPrecise>
+__device__ __forceinline__ bool test_leaf(const Tri* __restrict__ tris,
+                                          const float4* __restrict__ tri_lo, const Ray& r,
+                                          int ref, unsigned long long& ntest) {
   const int s0 = leaf_start(ref), cnt = leaf_count(ref);
   for (int k = s0; k < s0 + cnt; k++) {
     if (kCount) ntest++;
     const float4 v0 = __ldg(&tris[k].v0);
     const float4 v1 = __ldg(&tris[k].v1);
     const float4 v2 = __ldg(&tris[k].v2);
-    if (tri_hit(r, v0, v1, v2)) return true;
+    if (kPrecise) {
+      const float4 l0 = __ldg(&tri_lo[3LL * k]);
+      const float4 l1 = __ldg(&tri_lo[3LL * k + 1]);
+      const float4 l2 = __ldg(&tri_lo[3LL * k + 2]);
+      if (tri_hit_hl(r, v0, v1, v2, l0, l1, l2)) return true;
+    } else {
+      if (tri_hit(r, v0, v1, v2)) return true;
+    }
   }
   return false;
 }
 
-template <bool kCount>
+template <bool kCount, bool kPrecise>
 __global__ void __launch_bounds__(kFlatBlock, 8)
     k_trace_flat(const DomainDesc* __restrict__ doms, int ndom, const int* __restrict__ order,
                  int total, int* __restrict__ work, unsigned long long* __restrict__ counters,
@@ -354,9 +398,11 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
   int stack[kStackDepth];
   const Node* nodes = nullptr;
   const Tri* tris = nullptr;
+  const float4* tri_lo = nullptr;
   int root = kEmptyRef;
   float tfar = 0.f;
   float ox = 0.f, oy = 0.f, oz = 0.f;
+  float olx = 0.f, oly = 0.f, olz = 0.f;
   Ray r;
   unsigned long long rays = 0, nvis = 0, ntest = 0;
 
@@ -384,6 +430,7 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
           cell = (int)(g - D.cell_offset);
           nodes = D.nodes;
           tris = D.tris;
+          if (kPrecise) tri_lo = D.tri_lo;
           root = D.root;
           tfar = D.tfar;
           // Cell frame, mo_lradtopo_horayzon.cpp:694-720.
@@ -396,9 +443,17 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
           V3 north{v_n.x - dp * normal.x, v_n.y - dp * normal.y, v_n.z - dp * normal.z};
           unit3(north);
           const V3 east = cross3(north, normal);
-          ox = (float)(q.x + normal.x * D.ray_org_elev);
-          oy = (float)(q.y + normal.y * D.ray_org_elev);
-          oz = (float)(q.z + normal.z * D.ray_org_elev);
+          const double o64x = q.x + normal.x * D.ray_org_elev;
+          const double o64y = q.y + normal.y * D.ray_org_elev;
+          const double o64z = q.z + normal.z * D.ray_org_elev;
+          ox = (float)o64x;
+          oy = (float)o64y;
+          oz = (float)o64z;
+          if (kPrecise) {
+            olx = (float)(o64x - (double)ox);
+            oly = (float)(o64y - (double)oy);
+            olz = (float)(o64z - (double)oz);
+          }
           sv[0][t] = normal.x; sv[1][t] = normal.y; sv[2][t] = normal.z;
           sv[3][t] = north.x; sv[4][t] = north.y; sv[5][t] = north.z;
           sv[6][t] = east.x; sv[7][t] = east.y; sv[8][t] = east.z;
@@ -486,7 +541,7 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
       const float dx = (float)(ecs.x * sv[9][t] + ecs.y * sv[0][t]);
       const float dy = (float)(ecs.x * sv[10][t] + ecs.y * sv[1][t]);
       const float dz = (float)(ecs.x * sv[11][t] + ecs.y * sv[2][t]);
-      r = make_ray(ox, oy, oz, dx, dy, dz, tfar);
+      r = make_ray(ox, oy, oz, dx, dy, dz, tfar, olx, oly, olz);
       ref = root;
       sp = 0;
       need = false;
@@ -504,7 +559,7 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
         hit = true;
       }
     } else if (ref != kEmptyRef) {
-      hit = test_leaf<kCount>(tris, r, ref, ntest);
+      hit = test_leaf<kCount, kPrecise>(tris, tri_lo, r, ref, ntest);
       if (hit) fin = true;
       else ref = sp > 0 ? stack[--sp] : kEmptyRef;
     }
@@ -639,30 +694,37 @@ cudaError_t cell_order(const double* cell_enu, int begin, int count, int id_offs
   return radix_sort_pairs(keys, order, keys_alt, vals_alt, count, 32, sort_scratch, s);
 }
 
-template <bool kCount>
+template <bool kCount, bool kPrecise>
 cudaError_t launch_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
                         int* work, unsigned long long* counters, int* err, int advance_min,
                         cudaStream_t s) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_flat<kCount>, kFlatBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_flat<kCount, kPrecise>,
+                                                kFlatBlock, 0);
   long long blocks = (long long)sms * (per_sm > 0 ? per_sm : 1);
   const long long needed = ((long long)total + kFlatBlock - 1) / kFlatBlock;
   if (blocks > needed) blocks = needed;
-  k_trace_flat<kCount><<<(unsigned)blocks, kFlatBlock, 0, s>>>(doms, ndom, order, total, work,
-                                                               counters, err, advance_min);
+  k_trace_flat<kCount, kPrecise><<<(unsigned)blocks, kFlatBlock, 0, s>>>(
+      doms, ndom, order, total, work, counters, err, advance_min);
   note_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
                        int* work, unsigned long long* counters, int* err, int advance_min,
-                       bool count_work, cudaStream_t s) {
+                       bool count_work, bool precise, cudaStream_t s) {
   if (total <= 0 || ndom <= 0) return cudaSuccess;
-  return count_work
-             ? launch_flat<true>(doms, ndom, order, total, work, counters, err, advance_min, s)
-             : launch_flat<false>(doms, ndom, order, total, work, counters, err, advance_min, s);
+  if (precise)
+    return count_work ? launch_flat<true, true>(doms, ndom, order, total, work, counters, err,
+                                                advance_min, s)
+                      : launch_flat<false, true>(doms, ndom, order, total, work, counters, err,
+                                                 advance_min, s);
+  return count_work ? launch_flat<true, false>(doms, ndom, order, total, work, counters, err,
+                                               advance_min, s)
+                    : launch_flat<false, false>(doms, ndom, order, total, work, counters, err,
+                                                advance_min, s);
 }
 
 cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s) {

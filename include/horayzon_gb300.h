@@ -54,7 +54,20 @@ typedef struct hz_options {
     int32_t kernel;          /* HZ_KERNEL_PERSISTENT (default) or HZ_KERNEL_PER_CELL */
     int32_t advance_min;     /* persistent kernel: lanes of a warp that must wait before
                                 the search state advances (1..32; 0 = library default) */
+    int32_t precision;       /* HZ_PRECISION_REFERENCE (default) or HZ_PRECISION_LOCAL */
 } hz_options;
+
+enum {
+    /* FP32 vertices and ray origins in one global ENU frame, as the reference
+       traces them (mo_lradtopo_horayzon.cpp:403-410, 715-720): identical rays
+       and hit decisions. */
+    HZ_PRECISION_REFERENCE = 0,
+    /* Vertices and ray origins kept as FP32 hi + lo pairs of their FP64 ENU
+       values; each ray intersects FP32 vectors relative to its cell's FP64
+       origin, which removes the centimetre-scale quantisation of the global
+       FP32 frame. Persistent kernel only. */
+    HZ_PRECISION_LOCAL = 1
+};
 
 enum {
     HZ_KERNEL_PERSISTENT = 0,  /* flattened persistent search, Morton-ordered cells */
