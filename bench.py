@@ -175,6 +175,56 @@ def cpu_sample_run(dom, target_ray_s: float):
             "wall_s": wall}
 
 
+def precision_report(dom, d_in, h_ref, s_ref, stream, sample=20000):
+    """Reference-frame vs local-frame arithmetic against the FP64 oracle."""
+    from horayzon_extpar_gb300 import _lib, horizon_svf_comp_device
+    from oracle import api as oracle
+    h_loc, s_loc, st = horizon_svf_comp_device(*d_in, *ARGS, stream=stream,
+                                               precision=_lib.HZ_PRECISION_LOCAL)
+    h_loc, s_loc = h_loc.cpu().numpy(), s_loc.cpu().numpy()
+    cells = np.sort(np.random.default_rng(7).choice(dom.ncell, min(sample, dom.ncell),
+                                                    replace=False))
+    h64, s64, _ = oracle.horizon_svf(*dom.inputs(), *ARGS, precision=1, cells=cells)
+
+    def stats(h, s):
+        dh = np.abs(h[:, cells] - h64[:, cells])
+        ds = np.abs(s[cells] - s64[cells])
+        return {"frac_evals_differing": float(np.mean(dh > 1e-9)),
+                "max_abs_deg": float(dh.max()), "mean_abs_deg": float(dh.mean()),
+                "max_abs_svf": float(ds.max()), "mean_abs_svf": float(ds.mean())}
+
+    d = np.abs(h_loc - h_ref)
+    return {"oracle": "FP64 vertices, rays and triangle test (oracle/hz_oracle.c)",
+            "sample_cells": int(cells.size),
+            "reference_frame_vs_fp64": stats(h_ref, s_ref),
+            "local_frame_vs_fp64": stats(h_loc, s_loc),
+            "local_vs_reference_frame": {"frac_within_0.25deg": float(np.mean(d <= 0.25)),
+                                         "frac_identical": float(np.mean(d <= 1e-9))},
+            "local_frame_trace_ms": st["ms_trace"]}
+
+
+def batch_report(args):
+    """64 uneven independent domains in one call (one persistent search)."""
+    from horayzon_extpar_gb300 import synthetic
+    from horayzon_extpar_gb300.horizon_svf import horizon_svf_comp_batch
+    batch = synthetic.make_batch(64, seed=0)
+    doms = [(d.inputs(), a) for d, a in batch]
+    evals = sum(d.ncell * a[0] for d, a in batch)
+    horizon_svf_comp_batch(doms)  # warm-up
+    t0 = time.perf_counter()
+    _, st = horizon_svf_comp_batch(doms, return_stats=True)
+    wall = time.perf_counter() - t0
+    lat = np.array(st["latency_ms"])
+    return {"workload": "64 domains, 10k-500k cells (log-uniform), 0.5-2.5 km, relief "
+                        "1000-4500 m, nhori in {16, 24, 36}",
+            "cells": int(sum(d.ncell for d, _ in batch)), "evals": int(evals),
+            "search_ms": st["ms_trace"], "evals_per_s_search": evals / (st["ms_trace"] * 1e-3),
+            "evals_per_s_e2e_host": evals / wall,
+            "latency_ms_p50": float(np.percentile(lat, 50)),
+            "latency_ms_p99": float(np.percentile(lat, 99)),
+            "kernel_launches": st["kernel_launches"]}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -307,6 +357,13 @@ def run_gpu(args):
     if not (np.isfinite(hz).all() and (sv > 0).all() and (sv <= 1).all()):
         raise RuntimeError("invalid outputs")
 
+    # Untimed extras: the local-precision mode and its error against the FP64
+    # oracle on a cell sample; the batched uneven-domain workload.
+    extras = {}
+    if not args.no_extras and rank == 0:
+        extras["precision"] = precision_report(dom, d_in, hz, sv, stream)
+        extras["batched_domains"] = batch_report(args)
+
     peak, peak_kind = measured_peaks()
     alg_bytes = BYTES_PER_NODE * st_count["node_visits"] + BYTES_PER_TRI * st_count["tri_tests"]
     achieved = alg_bytes / (trace_ms * 1e-3) / 1e9
@@ -359,6 +416,7 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": (launches * args.steps) if launches else None,
+        **extras,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -375,6 +433,8 @@ def main():
     ap.add_argument("--box-km", type=float, default=600.0,
                     help="domain width (600 = the benchmark workload; smaller for profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the precision report and the batched-domain run")
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="target seconds of CPU ray work per CPU measurement")
     args = ap.parse_args()

@@ -502,7 +502,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     if (total > INT32_MAX) return fail(HZ_ERR_VALUE, "more than 2^31 cells in one call");
     HZ_CUDA(cudaMemcpyAsync(bb.doms, desc, sizeof(DomainDesc) * (size_t)n,
                             cudaMemcpyHostToDevice, s));
-    const int adv = opt.advance_min >= 1 && opt.advance_min <= 32 ? opt.advance_min : 16;
+    const int adv = opt.advance_min >= 1 && opt.advance_min <= 32 ? opt.advance_min : 24;
     k_stamp<<<1, 1, 0, s>>>(bb.t0);
     note_launches(1);
     HZ_CUDA(cudaGetLastError());
