@@ -22,7 +22,8 @@ HZ_OK, HZ_ERR_VALUE, HZ_ERR_TYPE, HZ_ERR_INDEX, HZ_ERR_CUDA, HZ_ERR_INTERNAL = r
 EXPORTED_SYMBOLS = ("hz_default_options", "horizon_svf_comp", "hz_horizon_svf",
                     "hz_horizon_svf_device", "hz_build_mesh", "hz_mesh_enu32",
                     "hz_last_error", "hz_version", "hz_release_workspace",
-                    "hz_horizon_svf_device_static", "hz_horizon_svf_batch")
+                    "hz_horizon_svf_device_static", "hz_horizon_svf_batch",
+                    "hz_mlp_num_params", "hz_mlp_train_step", "hz_mlp_forward")
 
 
 class Domain(C.Structure):
@@ -42,7 +43,9 @@ class Options(C.Structure):
                 ("verbose", C.c_int32), ("elev_floor_deg", C.c_double),
                 ("cell_begin", C.c_int32), ("cell_count", C.c_int32),
                 ("kernel", C.c_int32), ("advance_min", C.c_int32),
-                ("precision", C.c_int32)]
+                ("precision", C.c_int32), ("mlp_params", C.c_void_p),
+                ("mlp_every_azimuth", C.c_int32), ("raw_index", C.c_void_p),
+                ("features", C.c_void_p)]
 
 
 HZ_KERNEL_PERSISTENT, HZ_KERNEL_PER_CELL = 0, 1
@@ -113,6 +116,13 @@ def load(build_if_missing: bool = True):
         L.hz_horizon_svf_batch.restype = C.c_int
         L.hz_horizon_svf_batch.argtypes = [C.POINTER(Domain), C.c_int, C.c_int, C.c_void_p,
                                            C.POINTER(Options), C.POINTER(Stats)]
+        L.hz_mlp_num_params.restype = C.c_int
+        L.hz_mlp_num_params.argtypes = []
+        L.hz_mlp_train_step.restype = C.c_int
+        L.hz_mlp_train_step.argtypes = [C.c_void_p] * 5 + [C.c_int, C.c_int, C.c_float] + \
+            [C.c_void_p] * 3
+        L.hz_mlp_forward.restype = C.c_int
+        L.hz_mlp_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         L.hz_build_mesh.restype = C.c_int
         L.hz_build_mesh.argtypes = [_D, _D, _D, _D, _D, _I, C.c_int, C.c_int, C.c_int,
                                     _D, _D, _D, C.c_int, _I, C.c_int,

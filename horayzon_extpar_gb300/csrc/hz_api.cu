@@ -88,6 +88,11 @@ struct Buffers {
   float* vert32;
   float* vert_lo;    // precise mode only
   float4* tri_lo;    // precise mode only
+  // learned warm start only
+  unsigned* rz_bits;
+  float* rz;
+  long long raster_budget;
+  int16_t* start_m;
   double* cell_enu;
   // BVH
   Node* nodes;
@@ -102,7 +107,8 @@ struct Buffers {
 };
 
 Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhori,
-                     int grid_type, bool host_io, bool precise = false) {
+                     int grid_type, bool host_io, bool precise = false, bool learned = false,
+                     long long L = 0) {
   Buffers b;
   std::memset(&b, 0, sizeof(b));
   const long long max_tri = (grid_type == 0 ? 4 : 6) * nvert;
@@ -137,6 +143,12 @@ Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhor
     b.vert_lo = c.take<float>(3 * max_mv);
     b.tri_lo = c.take<float4>(3 * nt);
   }
+  if (learned) {
+    b.raster_budget = max_mv + max_mv / 10 + 4096;
+    b.rz_bits = c.take<unsigned>(b.raster_budget);
+    b.rz = c.take<float>(b.raster_budget);
+    b.start_m = c.take<int16_t>(L * ncell);
+  }
   b.bvh.keys = c.take<uint32_t>(nt);
   b.bvh.vals = c.take<int32_t>(nt);
   b.bvh.keys_alt = c.take<uint32_t>(nt);
@@ -165,10 +177,12 @@ struct BatchBuffers {
   unsigned long long* done;       // per domain: finished cells, completion time
   unsigned long long* t0;         // globaltimer at the start of the search
   int* err;
+  float* mlp;                     // learned warm start parameters (device copy)
 };
 
 BatchBuffers carve_batch(Carver& c, int n, long long total_cells) {
   BatchBuffers b;
+  b.mlp = c.take<float>(kMlpParams);
   b.doms = c.take<DomainDesc>(n);
   b.order = c.take<int32_t>(total_cells);
   b.work = c.take<int>(4);
@@ -462,12 +476,78 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     HZ_CUDA(trace_exact(p, opt.count_work != 0, s));
   } else {
     DomainDesc* desc = reinterpret_cast<DomainDesc*>(pin + 64 + 5 * (size_t)n + 8);
+    // Learned warm start: height rasters over each domain's triangle-centre
+    // bounds (read back from the BVH build), then features + MLP.
+    const bool learned = b[0].rz != nullptr;
+    std::vector<RasterDesc> rdesc(n);
+    if (learned) {
+      if (opt.mlp_params)
+        HZ_CUDA(cudaMemcpyAsync(bb.mlp, opt.mlp_params, sizeof(float) * kMlpParams,
+                                cudaMemcpyHostToDevice, s));
+      unsigned* pb = reinterpret_cast<unsigned*>(pin + 64 + 2 * n);  // 4 per domain
+      for (int d = 0; d < n; d++)
+        if (out->n_tri[d] > 0)
+          HZ_CUDA(cudaMemcpyAsync(pb + 4 * d, b[d].bvh.bounds, 4 * sizeof(unsigned),
+                                  cudaMemcpyDeviceToHost, s));
+      HZ_CUDA(cudaStreamSynchronize(s));
+      for (int d = 0; d < n; d++) {
+        RasterDesc R;
+        std::memset(&R, 0, sizeof(R));
+        R.nx = R.ny = 1;
+        R.dx = R.inv_dx = 1.f;
+        if (out->n_tri[d] > 0) {
+          const float x0 = ord2f_host(pb[4 * d]), y0 = ord2f_host(pb[4 * d + 1]);
+          const float x1 = ord2f_host(pb[4 * d + 2]), y1 = ord2f_host(pb[4 * d + 3]);
+          const double ex = std::max(1.0, (double)x1 - x0), ey = std::max(1.0, (double)y1 - y0);
+          double dx = sqrt(ex * ey / (0.9 * (double)b[d].raster_budget));
+          for (;;) {
+            const long long nx = (long long)ceil(ex / dx) + 8, ny = (long long)ceil(ey / dx) + 8;
+            if (nx * ny <= b[d].raster_budget) {
+              R.nx = (int)nx;
+              R.ny = (int)ny;
+              break;
+            }
+            dx *= 1.05;
+          }
+          R.dx = (float)dx;
+          R.inv_dx = (float)(1.0 / dx);
+          R.x0 = (float)(x0 - 4.0 * dx);
+          R.y0 = (float)(y0 - 4.0 * dx);
+        }
+        R.z = b[d].rz;
+        rdesc[d] = R;
+      }
+    }
     long long total = 0;
     for (int d = 0; d < n; d++) {
       const Problem& P = pr[d];
       const int L = P.nhori * P.refine;
       HZ_CUDA(trace_tables(b[d].azim_cs, b[d].elev_cs, b[d].sin_lattice, L, shift[d],
                            hori_acc, s));
+      if (learned) {
+        HZ_CUDA(raster_build(b[d].vert32, b[d].vot, out->n_tri[d], rdesc[d], b[d].rz_bits,
+                             b[d].rz, s));
+        LearnParams q;
+        std::memset(&q, 0, sizeof(q));
+        q.cell_enu = b[d].cell_enu;
+        q.centre = frames[d].centre;
+        q.pole = frames[d].pole;
+        q.ray_org_elev = P.ray_org_elev;
+        q.ncell = P.ncell;
+        q.cell_begin = P.cell_begin;
+        q.cell_count = P.cell_count;
+        q.nhori = P.nhori;
+        q.L = L;
+        // Predictions feed the first azimuth only unless every azimuth uses
+        // them; features for training cover every azimuth.
+        q.L_pred = (opt.features != nullptr && n == 1) || opt.mlp_every_azimuth ? L : 1;
+        q.dist_search = (float)P.dist_search;
+        q.azim_cs = b[d].azim_cs;
+        q.raster = rdesc[d];
+        q.features = n == 1 ? opt.features : nullptr;
+        q.start_m = b[d].start_m;
+        HZ_CUDA(learn_features(q, opt.mlp_params ? bb.mlp : nullptr, s));
+      }
       HZ_CUDA(cell_order(b[d].cell_enu, P.cell_begin, P.cell_count, (int)(total - P.cell_begin),
                          bb.order + total, b[d].order_scratch, b[d].cell_bounds, bb.work, s));
       DomainDesc D;
@@ -482,6 +562,9 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.elev_cs = b[d].elev_cs;
       D.sin_lattice = b[d].sin_lattice;
       D.done = n > 1 ? bb.done + 2 * d : nullptr;
+      D.start_m = opt.mlp_params ? b[d].start_m : nullptr;
+      D.start_all = opt.mlp_every_azimuth ? 1 : 0;
+      D.raw_j = n == 1 ? opt.raw_index : nullptr;
       D.centre = frames[d].centre;
       D.pole = frames[d].pole;
       D.ray_org_elev = P.ray_org_elev;
@@ -647,10 +730,16 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
   const bool precise = opt.precision == HZ_PRECISION_LOCAL;
   if (precise && opt.kernel == HZ_KERNEL_PER_CELL)
     return fail(HZ_ERR_VALUE, "HZ_PRECISION_LOCAL needs the persistent kernel");
+  const bool learned = opt.mlp_params != nullptr || opt.features != nullptr;
+  if (learned && opt.kernel == HZ_KERNEL_PER_CELL)
+    return fail(HZ_ERR_VALUE, "the learned warm start needs the persistent kernel");
+  if ((opt.raw_index || opt.features) && (n != 1 || !on_device))
+    return fail(HZ_ERR_VALUE, "raw_index / features are outputs of the device entry point");
   Carver dry(nullptr);
   for (int d = 0; d < n; d++)
     carve_domain(dry, doms[d].num_cell, doms[d].num_vertex, doms[d].num_hori,
-                 doms[d].grid_type, !on_device, precise);
+                 doms[d].grid_type, !on_device, precise, learned,
+                 (long long)doms[d].num_hori * doms[d].refine_factor);
   carve_batch(dry, n, total_cells);
   rc = E->reserve(dry.off, s);
   if (rc) return rc;
@@ -658,7 +747,8 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
   std::vector<Buffers> b(n);
   for (int d = 0; d < n; d++)
     b[d] = carve_domain(c, doms[d].num_cell, doms[d].num_vertex, doms[d].num_hori,
-                        doms[d].grid_type, !on_device, precise);
+                        doms[d].grid_type, !on_device, precise, learned,
+                        (long long)doms[d].num_hori * doms[d].refine_factor);
   const BatchBuffers bb = carve_batch(c, n, total_cells);
 
   std::vector<Problem> pr(n);
@@ -807,6 +897,37 @@ int hz_horizon_svf(const double* clon, const double* clat, const double* hsurf,
                             num_cell, num_vertex, num_hori, grid_type, dist_search,
                             ray_org_elev, refine_factor, svf_type);
   return run_entry(&h, 1, false, nullptr, opt, stats);
+}
+
+int hz_mlp_num_params(void) { return kMlpParams; }
+
+int hz_mlp_train_step(float* params, float* adam_m, float* adam_v, const float* X,
+                      const float* T, int n, int step, float lr, float* loss, float* grads,
+                      void* stream) {
+  g_last_error.clear();
+  if (!params || !X || !T || !loss || !grads || n < 1 || step < 1 ||
+      (lr > 0.f && (!adam_m || !adam_v)))
+    return fail(HZ_ERR_VALUE, "invalid MLP training arguments");
+  Engine* E = nullptr;
+  int rc = get_engine(-1, &E);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(E->mu);
+  cudaStream_t s = (cudaStream_t)stream;
+  rc = E->reserve(sizeof(float) * mlp_train_scratch_floats(n), s);
+  if (rc) return rc;
+  HZ_CUDA(mlp_train_step(params, adam_m, adam_v, X, T, n, step, lr, loss, grads,
+                         (float*)E->arena, s));
+  HZ_CUDA(cudaStreamSynchronize(s));
+  return HZ_OK;
+}
+
+int hz_mlp_forward(const float* params, const float* X, int n, float* Y, void* stream) {
+  g_last_error.clear();
+  if (!params || !X || !Y || n < 0) return fail(HZ_ERR_VALUE, "invalid MLP arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  HZ_CUDA(mlp_forward(params, X, n, Y, s));
+  HZ_CUDA(cudaStreamSynchronize(s));
+  return HZ_OK;
 }
 
 int hz_horizon_svf_batch(hz_domain* domains, int n_domains, int on_device, void* stream,

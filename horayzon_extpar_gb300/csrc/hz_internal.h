@@ -131,6 +131,9 @@ struct DomainDesc {
   const double2* elev_cs;
   const double* sin_lattice;
   unsigned long long* done;   // optional: [0] finished cells, [1] globaltimer at the last
+  const int16_t* start_m;     // optional learned start lattice index [L][ncell]
+  int start_all;              // 1: learned start at every azimuth; 0: azimuth 0 only
+  int16_t* raw_j;             // optional output: unclipped horizon j (h = j * 0.25 deg)
   double3 centre, pole;       // Earth centre / North Pole in ENU
   double ray_org_elev, hori_acc, elev_floor;
   long long cell_offset;      // work id of cell 0 of this domain
@@ -145,5 +148,46 @@ struct DomainDesc {
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
                        int* work, unsigned long long* counters, int* err, int advance_min,
                        bool count_work, bool precise, cudaStream_t s);
+
+// ---- hz_learn.cu ------------------------------------------------------------
+constexpr int kMlpIn = 32;
+constexpr int kMlpHidden = 64;
+constexpr int kMlpParams = kMlpIn * kMlpHidden + kMlpHidden + kMlpHidden * kMlpHidden +
+                           kMlpHidden + kMlpHidden + 1;  // 6337
+constexpr int kMlpStartMin = -170;  // -85 deg
+constexpr int kMlpStartMax = 180;   // +90 deg
+
+// Height field of a domain on a regular grid of its ENU x/y plane.
+struct RasterDesc {
+  float x0, y0, dx, inv_dx;
+  int nx, ny;
+  const float* z;  // [ny][nx], -inf where no triangle covers the texel
+};
+
+struct LearnParams {
+  const double* cell_enu;
+  double3 centre, pole;
+  double ray_org_elev;
+  int ncell, cell_begin, cell_count, nhori, L;
+  int L_pred;        // azimuths 0 .. L_pred - 1 get features / predictions
+  float dist_search;
+  const double2* azim_cs;
+  RasterDesc raster;
+  float* features;   // optional [L][ncell][32]
+  int16_t* start_m;  // with params: learned start lattice index [L][ncell]
+};
+
+cudaError_t raster_build(const float* vert32, const int* vot, int n_tri, RasterDesc R,
+                         unsigned* zbits, float* z, cudaStream_t s);
+// Features of every traced (cell, azimuth); with params (FP32, kMlpParams,
+// device) also the MLP's start index.
+cudaError_t learn_features(const LearnParams& q, const float* params, cudaStream_t s);
+size_t mlp_train_scratch_floats(int n);
+// One step on n samples: gradients to grads[kMlpParams]; with lr > 0 an Adam
+// update of params (step counts from 1).
+cudaError_t mlp_train_step(float* params, float* adam_m, float* adam_v, const float* X,
+                           const float* T, int n, int step, float lr, float* loss,
+                           float* grads, float* scratch, cudaStream_t s);
+cudaError_t mlp_forward(const float* params, const float* X, int n, float* Y, cudaStream_t s);
 
 }  // namespace hz

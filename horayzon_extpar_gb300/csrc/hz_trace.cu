@@ -489,6 +489,7 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
           // cpp:535/546, then the clip / sector / SVF epilogue of cpp:736-754.
           double h = phase == kPhaseUp ? elev - ha : elev + ha;
           const int j = phase == kPhaseUp ? 2 * m - 1 : 2 * m + 1;  // h ~ j * ha
+          if (D.raw_j) D.raw_j[(long long)a * D.ncell + cell] = (int16_t)j;
           if (h < 0.0) h = 0.0;
           double sector = sv[13][t] + h;
           if ((a + 1) % D.refine == 0) {
@@ -521,8 +522,13 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
           sv[14][t] = svf;
           phase = kPhaseFirst;
         }
-        // New azimuth (the elevation carries over, cpp:511): horizontal
-        // direction cos(theta_a) N + sin(theta_a) E.
+        // New azimuth: the elevation carries over (cpp:511), or starts at the
+        // learned proposal; horizontal direction cos(theta_a) N + sin(theta_a) E.
+        const int16_t* start_m = doms[dom].start_m;
+        if (start_m && (a == 0 || doms[dom].start_all)) {
+          m = start_m[(long long)a * doms[dom].ncell + cell];
+          sv[12][t] = (double)m * (2.0 * doms[dom].hori_acc);
+        }
         const double2 cs = __ldg(&doms[dom].azim_cs[a]);
         sv[9][t] = cs.x * sv[3][t] + cs.y * sv[6][t];
         sv[10][t] = cs.x * sv[4][t] + cs.y * sv[7][t];

@@ -72,20 +72,35 @@ def _check_args(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_t
 
 
 def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
-             advance_min=0, precision=0):
+             advance_min=0, precision=0, mlp_params=None, raw_index=None, features=None,
+             mlp_every_azimuth=False):
     begin, count = (0, 0) if cells is None else (int(cells[0]), int(cells[1]) - int(cells[0]))
-    return _lib.default_options(device=int(device), count_work=int(bool(count_work)),
-                                elev_floor_deg=float(elev_floor_deg),
-                                verbose=int(bool(verbose)), cell_begin=begin,
-                                cell_count=count, kernel=int(kernel),
-                                advance_min=int(advance_min), precision=int(precision))
+    opt = _lib.default_options(device=int(device), count_work=int(bool(count_work)),
+                               elev_floor_deg=float(elev_floor_deg),
+                               verbose=int(bool(verbose)), cell_begin=begin,
+                               cell_count=count, kernel=int(kernel),
+                               advance_min=int(advance_min), precision=int(precision))
+    if mlp_params is not None:
+        p = np.ascontiguousarray(mlp_params, dtype=np.float32)
+        if p.size != _lib.load().hz_mlp_num_params():
+            raise ValueError("mlp_params must hold %d values"
+                             % _lib.load().hz_mlp_num_params())
+        opt._keep = p  # alive for the duration of the call
+        opt.mlp_params = p.ctypes.data
+        opt.mlp_every_azimuth = int(bool(mlp_every_azimuth))
+    if raw_index is not None:
+        opt.raw_index = raw_index.data_ptr()
+    if features is not None:
+        opt.features = features.data_ptr()
+    return opt
 
 
 def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori,
                         grid_type, dist_search, ray_org_elev, refine_factor, svf_type,
                         *, device=-1, count_work=False, elev_floor_deg=-85.0,
                         verbose=False, return_stats=False, cells=None, kernel=0,
-                        advance_min=0, precision=0):
+                        advance_min=0, precision=0, mlp_params=None,
+                        mlp_every_azimuth=False):
     """Compute the terrain horizon and sky view factor on the GPU.
 
     Arguments and returns as horizon_svf.pyx:15-76: FP64 1-D ``clon, clat``
@@ -122,7 +137,7 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
     cells_of_vertex = np.ascontiguousarray(cells_of_vertex)
     L = _lib.load()
     opt = _options(device, count_work, elev_floor_deg, verbose, cells, kernel, advance_min,
-                   precision)
+                   precision, mlp_params, mlp_every_azimuth=mlp_every_azimuth)
     st = _lib.Stats()
     rc = L.hz_horizon_svf(clon.ctypes.data_as(_D), clat.ctypes.data_as(_D),
                           hsurf.ctypes.data_as(_D), vlon.ctypes.data_as(_D),
@@ -141,7 +156,8 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
                             grid_type, dist_search, ray_org_elev, refine_factor,
                             svf_type, horizon=None, skyview=None, *, stream=None,
                             count_work=False, elev_floor_deg=-85.0, cells=None, kernel=0,
-                            advance_min=0, precision=0):
+                            advance_min=0, precision=0, mlp_params=None, raw_index=None,
+                            features=None, mlp_every_azimuth=False):
     """Same computation on CUDA tensors (torch) already resident on one GPU.
 
     Inputs: contiguous float64 / int32 tensors on the same device, layouts as
@@ -177,7 +193,8 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
         stream = torch.cuda.current_stream(dev)
     L = _lib.load()
     opt = _options(dev.index if dev.index is not None else -1, count_work,
-                   elev_floor_deg, False, cells, kernel, advance_min, precision)
+                   elev_floor_deg, False, cells, kernel, advance_min, precision, mlp_params,
+                   raw_index, features, mlp_every_azimuth)
     st = _lib.Stats()
     rc = L.hz_horizon_svf_device(clon.data_ptr(), clat.data_ptr(), hsurf.data_ptr(),
                                  vlon.data_ptr(), vlat.data_ptr(),
@@ -231,7 +248,8 @@ def mesh_enu32(clon, clat, hsurf, vlon, vlat, cells_of_vertex, grid_type, device
 
 
 def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_deg=-85.0,
-                           advance_min=0, return_stats=False, precision=0):
+                           advance_min=0, return_stats=False, precision=0, mlp_params=None,
+                           mlp_every_azimuth=False):
     """Many independent domains in one call (one persistent search launch).
 
     ``domains``: sequence of ``(inputs, args)`` with ``inputs`` the six arrays
@@ -257,7 +275,8 @@ def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_d
             arrs[0].size, arrs[3].size, int(num_hori), int(grid_type), float(dist_search),
             float(ray_org_elev), int(refine), int(svf), 0.0))
     arr = (_lib.Domain * len(structs))(*structs)
-    opt = _options(device, count_work, elev_floor_deg, False, None, 0, advance_min, precision)
+    opt = _options(device, count_work, elev_floor_deg, False, None, 0, advance_min, precision,
+                   mlp_params, mlp_every_azimuth=mlp_every_azimuth)
     st = _lib.Stats()
     rc = _lib.load().hz_horizon_svf_batch(arr, len(structs), 0, None, C.byref(opt),
                                           C.byref(st))

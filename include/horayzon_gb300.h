@@ -55,6 +55,20 @@ typedef struct hz_options {
     int32_t advance_min;     /* persistent kernel: lanes of a warp that must wait before
                                 the search state advances (1..32; 0 = library default) */
     int32_t precision;       /* HZ_PRECISION_REFERENCE (default) or HZ_PRECISION_LOCAL */
+    /* Learned warm start: host pointer to hz_mlp_num_params() FP32 parameters
+       of the 32-64-64-1 MLP, or NULL for the reference's chained start. The
+       bracket of the first azimuth of every cell (which the reference starts
+       at 0 deg, cpp:511) -- or, with mlp_every_azimuth, of every azimuth --
+       then starts at the MLP's proposal, and the same bracketing search
+       refines it. Persistent kernel only. */
+    const float* mlp_params;
+    int32_t mlp_every_azimuth;
+    /* Device outputs for training data (hz_horizon_svf_device, one domain):
+       raw_index [L][num_cell] int16, the unclipped horizon of every azimuth in
+       quarter degrees; features [L][num_cell][32] float, the MLP inputs. L =
+       num_hori * refine_factor. NULL = not written. */
+    int16_t* raw_index;
+    float* features;
 } hz_options;
 
 enum {
@@ -218,6 +232,24 @@ int hz_horizon_svf_device_static(const double* clon, const double* clat,
                                  int grid_type, double dist_search,
                                  double ray_org_elev, int refine_factor, int svf_type,
                                  void* stream);
+
+/*
+ * Learned warm start, no reference counterpart. Parameters are packed FP32:
+ * W1[32][64], b1[64], W2[64][64], b2[64], W3[64], b3; the forward pass rounds
+ * them to BF16 and accumulates in FP32 (ReLU hidden layers). Targets are the
+ * horizon in units of 8 deg (quarter-degree index / 32). All arrays are
+ * device pointers; work runs on `stream` and the call returns when it is done.
+ */
+int hz_mlp_num_params(void);
+/* One training step on n samples X[n][32], T[n]: writes the mean-squared-error
+ * loss to *loss and the gradient to grads[hz_mlp_num_params()]; with lr > 0
+ * also an Adam step (beta 0.9 / 0.999, eps 1e-8, step >= 1) on params using
+ * the moment buffers adam_m, adam_v. */
+int hz_mlp_train_step(float* params, float* adam_m, float* adam_v, const float* X,
+                      const float* T, int n, int step, float lr, float* loss, float* grads,
+                      void* stream);
+/* Y[n] = MLP(X[n][32]). */
+int hz_mlp_forward(const float* params, const float* X, int n, float* Y, void* stream);
 
 /* Message of the last failed call on this thread ("" if none). */
 const char* hz_last_error(void);

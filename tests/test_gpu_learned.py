@@ -1,0 +1,112 @@
+"""Learned warm start: the GPU MLP kernels against the FP64 numpy oracle
+(forward, loss, gradients), training, and what the trained network changes
+in the search (same results within the parity bar, fewer rays than an
+untrained network)."""
+import numpy as np
+import pytest
+
+from horayzon_extpar_gb300 import horizon_svf_comp_py, learned, synthetic
+from oracle import mlp_ref
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+def _batch(torch, n, seed):
+    rng = np.random.default_rng(seed)
+    X = rng.normal(0, 1, (n, 32)).astype(np.float32)
+    T = (np.tanh(X[:, :4].sum(1)) + 0.1 * rng.normal(size=n)).astype(np.float32)
+    dev = torch.device("cuda:0")
+    return X, T, torch.from_numpy(X).to(dev), torch.from_numpy(T).to(dev)
+
+
+def test_mlp_forward_and_gradients_match_fp64_oracle(torch):
+    p = mlp_ref.bf16_round(learned.init_params(3) + 0.01)
+    X, T, Xd, Td = _batch(torch, 700, 1)
+    y_ref, _ = mlp_ref.forward(p, X)
+    y = learned.forward(p, Xd).cpu().numpy()
+    np.testing.assert_allclose(y, y_ref, rtol=1e-4, atol=1e-4)
+    loss_ref, g_ref = mlp_ref.loss_and_grad(p, X, T)
+    loss, g = learned.gradients(p, Xd, Td)
+    assert abs(loss - loss_ref) <= 1e-4 * max(1.0, loss_ref)
+    scale = np.abs(g_ref).max()
+    np.testing.assert_allclose(g, g_ref, rtol=2e-3, atol=1e-5 * scale)
+
+
+def test_mlp_weights_are_rounded_to_bf16(torch):
+    p = learned.init_params(5)
+    X, _, Xd, _ = _batch(torch, 64, 2)
+    y = learned.forward(p, Xd).cpu().numpy()
+    y_bf, _ = mlp_ref.forward(mlp_ref.bf16_round(p), X)
+    np.testing.assert_allclose(y, y_bf, rtol=1e-4, atol=1e-4)
+
+
+def test_training_reduces_loss(torch):
+    _, _, Xd, Td = _batch(torch, 20000, 3)
+    p0 = learned.init_params(0)
+    l0, _ = learned.gradients(p0, Xd, Td)
+    p1, hist = learned.train(Xd, Td, steps=300, batch=4096, lr=3e-3, seed=1)
+    l1, _ = learned.gradients(p1, Xd, Td)
+    assert l1 < 0.3 * l0
+
+
+@pytest.fixture(scope="module")
+def trained(torch):
+    """An MLP trained on the plain method's horizons of two other seeds."""
+    kw = dict(edge_km=0.5, box_km=40.0, kind="eroded", hmin=500.0, hmax=4200.0, n_features=0)
+    args = (24, 1, 8000.0, 0.2, 1, 2)
+    Xs, Ts = [], []
+    for seed in (101, 102):
+        X, T = learned.training_samples(synthetic.make_domain(seed=seed, **kw), args,
+                                        max_samples=400000)
+        Xs.append(X)
+        Ts.append(T)
+    X = torch.cat(Xs)
+    T = torch.cat(Ts)
+    p, _ = learned.train(X, T, steps=1500, batch=16384, lr=2e-3, seed=0)
+    return p, kw, args
+
+
+def test_learned_start_keeps_results_and_saves_rays(trained):
+    """First-azimuth learned start (the reference starts every cell at 0 deg):
+    same horizons within the parity bar, fewer rays than the plain chain and
+    than an untrained network. Every-azimuth mode: within the parity bar."""
+    p, kw, args = trained
+    d = synthetic.make_domain(seed=7, **kw)
+    # Results can change only where visibility is not monotone in elevation
+    # (the bracket's result then depends on where it starts). With the
+    # reference's global FP32 frame that happens at ray origins the FP32
+    # rounding puts under a steep neighbouring triangle; the local-precision
+    # frame removes those, so the comparison runs there.
+    loc = dict(precision=1, return_stats=True)
+    h0, s0, st0 = horizon_svf_comp_py(*d.inputs(), *args, **loc)
+    h1, s1, st1 = horizon_svf_comp_py(*d.inputs(), *args, mlp_params=p, **loc)
+    hu, su, stu = horizon_svf_comp_py(*d.inputs(), *args, mlp_params=learned.init_params(0),
+                                      **loc)
+    he, se, ste = horizon_svf_comp_py(*d.inputs(), *args, mlp_params=p,
+                                      mlp_every_azimuth=True, **loc)
+    def agree(h, s):
+        return (float(np.mean(np.abs(h - h0) <= 0.25)),
+                float(np.mean(np.abs(s - s0) <= 1e-3)))
+
+    stats = {"learned": agree(h1, s1), "untrained": agree(hu, su), "every": agree(he, se)}
+    print("agreement with the plain search (horizons within 0.25 deg, cells within "
+          "SVF 1e-3):", stats)
+    for k in ("learned", "untrained"):  # first azimuth from the MLP, then chained
+        assert stats[k][0] >= 0.999 and stats[k][1] >= 0.999, stats
+    assert stats["every"][0] >= 0.995, stats  # every azimuth restarted: more exposure
+    # Reference frame: the parity bar on the horizons.
+    hr0, _ = horizon_svf_comp_py(*d.inputs(), *args)
+    hr1, _ = horizon_svf_comp_py(*d.inputs(), *args, mlp_params=p)
+    assert np.mean(np.abs(hr1 - hr0) <= 0.25) >= 0.999
+    evals = d.ncell * args[0]
+    r = {k: st["num_rays"] / evals for k, st in
+         (("plain", st0), ("learned", st1), ("untrained", stu), ("every", ste))}
+    print("rays/eval", r)
+    assert r["learned"] < r["plain"]
+    assert r["learned"] < r["untrained"]
+    assert r["every"] >= 2.0 - 1e-9  # a bracket always needs a hit and a miss
