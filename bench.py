@@ -203,6 +203,58 @@ def precision_report(dom, d_in, h_ref, s_ref, stream, sample=20000):
             "local_frame_trace_ms": st["ms_trace"]}
 
 
+def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args):
+    """Learned warm start vs the plain chained search on the same workload.
+
+    The MLP is trained first (untimed) on the plain method's horizons of 8
+    other terrain seeds of the same recipe (60 x 60 km boxes), on the GPU with
+    the library's own kernels."""
+    import torch
+
+    from horayzon_extpar_gb300 import horizon_svf_comp_device, learned, synthetic
+    t0 = time.perf_counter()
+    Xs, Ts = [], []
+    for seed in range(1, 9):
+        d = synthetic.make_config("c3", seed=1000 + seed, box_km=min(60.0, args.box_km))
+        X, T = learned.training_samples(d, ARGS, max_samples=1_000_000, seed=seed)
+        Xs.append(X)
+        Ts.append(T)
+    X, T = torch.cat(Xs), torch.cat(Ts)
+    params, hist = learned.train(X, T, steps=3000, batch=32768, lr=2e-3, seed=0,
+                                 log_every=1000)
+    del X, T, Xs, Ts
+    train_s = time.perf_counter() - t0
+    out = {"training": {"seeds": "8 other seeds, 60 x 60 km boxes of the same recipe",
+                        "samples": 8_000_000, "steps": 3000, "batch": 32768,
+                        "seconds": train_s, "loss_history": hist}}
+    evals = dom.ncell * ARGS[0]
+    for mode, every in (("first_azimuth", False), ("every_azimuth", True)):
+        for _ in range(max(1, args.warmup)):
+            horizon_svf_comp_device(*d_in, *ARGS, stream=stream, mlp_params=params,
+                                    mlp_every_azimuth=every)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        rays = 0
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            h, s, st = horizon_svf_comp_device(*d_in, *ARGS, stream=stream, mlp_params=params,
+                                               mlp_every_azimuth=every)
+            ev[k][1].record(stream)
+            rays = st["num_rays"]
+        torch.cuda.synchronize()
+        ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+        dh = np.abs(h.cpu().numpy() - h_ref)
+        ds = np.abs(s.cpu().numpy() - s_ref)
+        out[mode] = {"value": evals / (ms * 1e-3), "unit": "evals/s", "ms_per_step": ms,
+                     "speedup_vs_plain": plain_ms / ms, "rays_per_eval": rays / evals,
+                     "agreement_with_plain": {
+                         "frac_within_0.25deg": float(np.mean(dh <= 0.25)),
+                         "frac_identical": float(np.mean(dh <= 1e-9)),
+                         "frac_cells_svf_within_1e-3": float(np.mean(ds <= 1e-3)),
+                         "max_abs_svf": float(ds.max())}}
+    return out
+
+
 def batch_report(args):
     """64 uneven independent domains in one call (one persistent search)."""
     from horayzon_extpar_gb300 import synthetic
@@ -361,6 +413,7 @@ def run_gpu(args):
     # oracle on a cell sample; the batched uneven-domain workload.
     extras = {}
     if not args.no_extras and rank == 0:
+        extras["learned"] = learned_report(dom, d_in, hz, sv, stream, ms, args)
         extras["precision"] = precision_report(dom, d_in, hz, sv, stream)
         extras["batched_domains"] = batch_report(args)
 
