@@ -75,9 +75,40 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def l2_read_peak(dev) -> float | None:
+    """L2 read bandwidth (GB/s) of this GPU from the project's probe kernel:
+    a 32 MiB buffer (L2 resident) streamed 300 times with L1-bypassing loads."""
+    import ctypes as C
+
+    import torch
+
+    from horayzon_extpar_gb300 import _build
+    path = _build.PROBE_PATH
+    if not os.path.exists(path):
+        path = _build.build_probe()
+    lib = C.CDLL(path)
+    lib.hz_probe_l2_read.restype = C.c_int
+    lib.hz_probe_l2_read.argtypes = [C.c_void_p, C.c_longlong, C.c_int, C.c_void_p,
+                                     C.c_void_p, C.POINTER(C.c_float)]
+    nbytes, reps = 32 << 20, 300
+    buf = torch.ones(nbytes // 4, dtype=torch.float32, device=dev)
+    sink = torch.zeros(4, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    best = None
+    for _ in range(3):
+        ms = C.c_float(0.0)
+        rc = lib.hz_probe_l2_read(buf.data_ptr(), nbytes, reps, sink.data_ptr(),
+                                  C.c_void_p(stream.cuda_stream), C.byref(ms))
+        if rc != 0 or ms.value <= 0:
+            return None
+        gbs = nbytes * reps / (ms.value * 1e-3) / 1e9
+        best = gbs if best is None else max(best, gbs)
+    return best
+
+
 def traffic_from_profile():
     """DRAM bytes per launch of the search kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_trace_flat_c3_500m.md")
+    path = os.path.join(ROOT, "profiles", "k_trace_warp_c3_500m.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -207,7 +238,7 @@ def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args):
     """Learned warm start vs the plain chained search on the same workload.
 
     The MLP is trained first (untimed) on the plain method's horizons of 8
-    other terrain seeds of the same recipe (60 x 60 km boxes), on the GPU with
+    other terrain seeds of the same recipe (120 x 120 km boxes), on the GPU with
     the library's own kernels."""
     import torch
 
@@ -215,7 +246,7 @@ def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args):
     t0 = time.perf_counter()
     Xs, Ts = [], []
     for seed in range(1, 9):
-        d = synthetic.make_config("c3", seed=1000 + seed, box_km=min(60.0, args.box_km))
+        d = synthetic.make_config("c3", seed=1000 + seed, box_km=min(120.0, args.box_km))
         X, T = learned.training_samples(d, ARGS, max_samples=1_000_000, seed=seed)
         Xs.append(X)
         Ts.append(T)
@@ -224,7 +255,7 @@ def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args):
                                  log_every=1000)
     del X, T, Xs, Ts
     train_s = time.perf_counter() - t0
-    out = {"training": {"seeds": "8 other seeds, 60 x 60 km boxes of the same recipe",
+    out = {"training": {"seeds": "8 other seeds, 120 x 120 km boxes of the same recipe",
                         "samples": 8_000_000, "steps": 3000, "batch": 32768,
                         "seconds": train_s, "loss_history": hist}}
     evals = dom.ncell * ARGS[0]
@@ -335,12 +366,17 @@ def run_gpu(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def step(count=False):
+    def step(count=False, kernel=_lib.HZ_KERNEL_PERSISTENT):
         return horizon_svf_comp_device(*d_in, *ARGS, horizon=horizon, skyview=skyview,
-                                       stream=stream, count_work=count)[2]
+                                       stream=stream, count_work=count, kernel=kernel)[2]
 
-    # Untimed: work counters of the same launch (node visits, triangle tests).
-    st_count = step(count=True)
+    # Untimed: work counters. The algorithmic bytes are defined on the binary
+    # LBVH (64 B per node visit, 48 B per triangle test), so they are counted
+    # by the same search on the BVH2; the 4-wide counts of the timed kernel
+    # are reported beside them.
+    st_count = step(count=True, kernel=_lib.HZ_KERNEL_PERSISTENT_BVH2)
+    st_wide = step(count=True)
+    l2_peak = l2_read_peak(dev)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -460,12 +496,18 @@ def run_gpu(args):
                      "trace": trace_ms},
         "e2e": {"value": world * evals / e2e_s, "unit": "evals/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "roofline": {"kernel": "k_trace_flat", "bound": "hbm", "achieved": achieved,
+        "roofline": {"kernel": "k_trace_warp", "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
                      "alg_bytes_per_launch": alg_bytes,
                      "node_visits_per_ray": st_count["node_visits"] / rays,
-                     "tri_tests_per_ray": st_count["tri_tests"] / rays},
+                     "tri_tests_per_ray": st_count["tri_tests"] / rays,
+                     "bvh4_node_visits_per_ray": st_wide["node_visits"] / rays,
+                     "bvh4_tri_tests_per_ray": st_wide["tri_tests"] / rays,
+                     "l2": {"peak": l2_peak, "unit": "GB/s",
+                            "frac": achieved / l2_peak if l2_peak else None,
+                            "peak_kind": "measured (hz_l2_probe: 32 MiB, 300 passes, "
+                                         "ld.global.cg)"}},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": (launches * args.steps) if launches else None,

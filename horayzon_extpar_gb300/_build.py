@@ -85,6 +85,25 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     return LIB_PATH
 
 
+PROBE_SRC = os.path.join(PKG, "probe", "hz_l2_probe.cu")
+PROBE_PATH = os.path.join(LIB_DIR, "libhz_probe.so")
+
+
+def build_probe(force: bool = False) -> str:
+    """The benchmark's L2 bandwidth probe (a separate small library)."""
+    os.makedirs(LIB_DIR, exist_ok=True)
+    if force or _stale(PROBE_PATH, [PROBE_SRC]):
+        tmp = PROBE_PATH + ".%d.tmp" % os.getpid()
+        cmd = [nvcc_path(), "-shared", "-o", tmp, PROBE_SRC, "-O3", "-std=c++17",
+               "-Xcompiler", "-fPIC", "-lcudart_static"] + ARCH
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("probe build failed: %s\n%s%s" % (" ".join(cmd), r.stdout,
+                                                                  r.stderr))
+        os.replace(tmp, PROBE_PATH)
+    return PROBE_PATH
+
+
 if __name__ == "__main__":
     import sys
     print(build_library(force="--force" in sys.argv, verbose="-v" in sys.argv))

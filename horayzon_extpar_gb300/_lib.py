@@ -45,10 +45,10 @@ class Options(C.Structure):
                 ("kernel", C.c_int32), ("advance_min", C.c_int32),
                 ("precision", C.c_int32), ("mlp_params", C.c_void_p),
                 ("mlp_every_azimuth", C.c_int32), ("raw_index", C.c_void_p),
-                ("features", C.c_void_p)]
+                ("features", C.c_void_p), ("leaf_min", C.c_int32)]
 
 
-HZ_KERNEL_PERSISTENT, HZ_KERNEL_PER_CELL = 0, 1
+HZ_KERNEL_PERSISTENT, HZ_KERNEL_PER_CELL, HZ_KERNEL_PERSISTENT_BVH2 = 0, 1, 2
 HZ_PRECISION_REFERENCE, HZ_PRECISION_LOCAL = 0, 1
 
 

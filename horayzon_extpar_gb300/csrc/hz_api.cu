@@ -96,6 +96,7 @@ struct Buffers {
   double* cell_enu;
   // BVH
   Node* nodes;
+  Node4* nodes4;     // wide traversal only
   Tri* tris;
   BvhScratch bvh;
   // search
@@ -106,9 +107,16 @@ struct Buffers {
   int* err;
 };
 
+// Traversal loop of the persistent search selected by hz_options.kernel.
+int trace_variant(const hz_options& opt) {
+  // HZ_KERNEL_PER_CELL runs single domains only; batches fall back to the
+  // persistent search on the binary BVH it builds.
+  return opt.kernel == HZ_KERNEL_PERSISTENT ? kTraceWide : kTraceBinary;
+}
+
 Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhori,
                      int grid_type, bool host_io, bool precise = false, bool learned = false,
-                     long long L = 0) {
+                     long long L = 0, bool wide = false) {
   Buffers b;
   std::memset(&b, 0, sizeof(b));
   const long long max_tri = (grid_type == 0 ? 4 : 6) * nvert;
@@ -138,6 +146,7 @@ Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhor
   b.cell_enu = c.take<double>(3 * ncell);
   const long long nt = max_tri > 0 ? max_tri : 1;
   b.nodes = c.take<Node>(nt > 1 ? nt - 1 : 1);
+  if (wide) b.nodes4 = c.take<Node4>(nt > 1 ? nt - 1 : 1);
   b.tris = c.take<Tri>(nt);
   if (precise) {
     b.vert_lo = c.take<float>(3 * max_mv);
@@ -429,7 +438,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   // ---- BVH (cpp:395-432) ----
   for (int d = 0; d < n; d++)
     HZ_CUDA(bvh_build(b[d].vert32, b[d].vot, out->n_tri[d], b[d].nodes, b[d].tris, b[d].bvh, s,
-                      b[d].vert_lo, b[d].tri_lo));
+                      b[d].vert_lo, b[d].tri_lo, b[d].nodes4));
   HZ_CUDA(cudaEventRecord(E.ev[2], s));
 
   // ---- horizon + SVF (cpp:651-761) ----
@@ -554,6 +563,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       std::memset(&D, 0, sizeof(D));
       D.cell_enu = b[d].cell_enu;
       D.nodes = b[d].nodes;
+      D.nodes4 = b[d].nodes4;
       D.tris = b[d].tris;
       D.tri_lo = b[d].tri_lo;
       D.horizon = P.horizon;
@@ -585,12 +595,15 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     if (total > INT32_MAX) return fail(HZ_ERR_VALUE, "more than 2^31 cells in one call");
     HZ_CUDA(cudaMemcpyAsync(bb.doms, desc, sizeof(DomainDesc) * (size_t)n,
                             cudaMemcpyHostToDevice, s));
-    const int adv = opt.advance_min >= 1 && opt.advance_min <= 32 ? opt.advance_min : 24;
+    const int adv =
+        opt.advance_min >= 1 && opt.advance_min <= 32 ? opt.advance_min : kDefaultAdvanceMin;
+    const int leaf = opt.leaf_min >= 1 && opt.leaf_min <= 32 ? opt.leaf_min : kDefaultLeafMin;
+    const int variant = trace_variant(opt);
     k_stamp<<<1, 1, 0, s>>>(bb.t0);
     note_launches(1);
     HZ_CUDA(cudaGetLastError());
     HZ_CUDA(trace_flat(bb.doms, n, bb.order, (int)total, bb.work, bb.counters, bb.err, adv,
-                       opt.count_work != 0, b[0].tri_lo != nullptr, s));
+                       leaf, variant, opt.count_work != 0, b[0].tri_lo != nullptr, s));
   }
   HZ_CUDA(cudaEventRecord(E.ev[3], s));
 
@@ -733,13 +746,16 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
   const bool learned = opt.mlp_params != nullptr || opt.features != nullptr;
   if (learned && opt.kernel == HZ_KERNEL_PER_CELL)
     return fail(HZ_ERR_VALUE, "the learned warm start needs the persistent kernel");
+  if (opt.kernel < HZ_KERNEL_PERSISTENT || opt.kernel > HZ_KERNEL_PERSISTENT_BVH2)
+    return fail(HZ_ERR_VALUE, "unknown kernel %d", opt.kernel);
+  const bool wide = opt.kernel != HZ_KERNEL_PER_CELL && trace_variant(opt) == kTraceWide;
   if ((opt.raw_index || opt.features) && (n != 1 || !on_device))
     return fail(HZ_ERR_VALUE, "raw_index / features are outputs of the device entry point");
   Carver dry(nullptr);
   for (int d = 0; d < n; d++)
     carve_domain(dry, doms[d].num_cell, doms[d].num_vertex, doms[d].num_hori,
                  doms[d].grid_type, !on_device, precise, learned,
-                 (long long)doms[d].num_hori * doms[d].refine_factor);
+                 (long long)doms[d].num_hori * doms[d].refine_factor, wide);
   carve_batch(dry, n, total_cells);
   rc = E->reserve(dry.off, s);
   if (rc) return rc;
@@ -748,7 +764,7 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
   for (int d = 0; d < n; d++)
     b[d] = carve_domain(c, doms[d].num_cell, doms[d].num_vertex, doms[d].num_hori,
                         doms[d].grid_type, !on_device, precise, learned,
-                        (long long)doms[d].num_hori * doms[d].refine_factor);
+                        (long long)doms[d].num_hori * doms[d].refine_factor, wide);
   const BatchBuffers bb = carve_batch(c, n, total_cells);
 
   std::vector<Problem> pr(n);

@@ -9,7 +9,8 @@
 //   4. k_karras: binary radix tree (Karras, HPG 2012) with index tie-break;
 //      subtrees of <= kLeafMax triangles become leaves;
 //   5. k_gather: 48-byte triangle records in leaf order;
-//   6. k_refit: bottom-up boxes with one atomic arrival counter per node.
+//   6. k_refit: bottom-up boxes with one atomic arrival counter per node;
+//   7. optionally k_collapse4: the 4-wide tree used by the wide traversal.
 // Child boxes carry a margin of 2^-20 x the largest coordinate so that box
 // culling never hides a triangle the watertight test would report. The tree
 // has the same topology as the CPU oracle's (same keys, same splits).
@@ -242,6 +243,52 @@ __global__ void k_small_root(Node* nodes, const Tri* __restrict__ tris, int n,
   nodes[0] = r;
 }
 
+// BVH4 node i from BVH2 node i: a leaf child stays, an internal child is
+// replaced by its two children (with the boxes that child stores for them).
+// Only live BVH2 nodes (ranges of more than kLeafMax triangles, or the single
+// root of a small tree) are converted.
+__global__ void k_collapse4(const Node* __restrict__ nodes, int n_nodes,
+                            const int* __restrict__ nsize, Node4* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_nodes || (nsize && nsize[i] <= kLeafMax)) return;
+  float lo[3][4], hi[3][4];
+  int ch[4];
+  int k = 0;
+  auto put = [&](int ref, float lx, float hx, float ly, float hy, float lz, float hz) {
+    ch[k] = ref;
+    lo[0][k] = lx; hi[0][k] = hx;
+    lo[1][k] = ly; hi[1][k] = hy;
+    lo[2][k] = lz; hi[2][k] = hz;
+    k++;
+  };
+  const Node n = nodes[i];
+  const int c[2] = {__float_as_int(n.d.x), __float_as_int(n.d.y)};
+  for (int side = 0; side < 2; side++) {
+    const int r = c[side];
+    if (r == kEmptyRef) continue;
+    if (r < 0) {
+      const float4 xy = side ? n.b : n.a;
+      put(r, xy.x, xy.y, xy.z, xy.w, side ? n.c.z : n.c.x, side ? n.c.w : n.c.y);
+    } else {
+      const Node m = nodes[r];
+      const int g0 = __float_as_int(m.d.x), g1 = __float_as_int(m.d.y);
+      put(g0, m.a.x, m.a.y, m.a.z, m.a.w, m.c.x, m.c.y);
+      if (g1 != kEmptyRef) put(g1, m.b.x, m.b.y, m.b.z, m.b.w, m.c.z, m.c.w);
+    }
+  }
+  while (k < 4) put(kEmptyRef, INFINITY, -INFINITY, INFINITY, -INFINITY, INFINITY, -INFINITY);
+  Node4 q;
+  q.lox = make_float4(lo[0][0], lo[0][1], lo[0][2], lo[0][3]);
+  q.hix = make_float4(hi[0][0], hi[0][1], hi[0][2], hi[0][3]);
+  q.loy = make_float4(lo[1][0], lo[1][1], lo[1][2], lo[1][3]);
+  q.hiy = make_float4(hi[1][0], hi[1][1], hi[1][2], hi[1][3]);
+  q.loz = make_float4(lo[2][0], lo[2][1], lo[2][2], lo[2][3]);
+  q.hiz = make_float4(hi[2][0], hi[2][1], hi[2][2], hi[2][3]);
+  q.child = make_int4(ch[0], ch[1], ch[2], ch[3]);
+  q.pad = make_int4(0, 0, 0, 0);
+  out[i] = q;
+}
+
 }  // namespace
 
 size_t bvh_scratch_bytes(long long n) {
@@ -257,7 +304,7 @@ size_t bvh_scratch_bytes(long long n) {
 
 cudaError_t bvh_build(const float* vert32, const int* vot, int n, Node* nodes, Tri* tris,
                       const BvhScratch& sc, cudaStream_t s, const float* vert_lo,
-                      float4* tri_lo) {
+                      float4* tri_lo, Node4* nodes4) {
   if (n <= 0) return cudaSuccess;
   k_init_bounds<<<1, 1, 0, s>>>(sc.bounds);
   k_tri_bounds<<<grid_for(n, 256), 256, 0, s>>>(vert32, vot, n, sc.cxy, sc.bounds);
@@ -271,6 +318,10 @@ cudaError_t bvh_build(const float* vert32, const int* vot, int n, Node* nodes, T
   if (n <= kLeafMax) {
     k_small_root<<<1, 1, 0, s>>>(nodes, tris, n, sc.bounds);
     note_launches(2);
+    if (nodes4) {
+      k_collapse4<<<1, 32, 0, s>>>(nodes, 1, nullptr, nodes4);
+      note_launches(1);
+    }
     return cudaGetLastError();
   }
   note_launches(3);
@@ -278,6 +329,10 @@ cudaError_t bvh_build(const float* vert32, const int* vot, int n, Node* nodes, T
                                                 sc.counter);
   k_refit<<<grid_for(n - 1, 256), 256, 0, s>>>(nodes, tris, n, sc.parent, sc.nsize,
                                                sc.counter, sc.bounds);
+  if (nodes4) {
+    k_collapse4<<<grid_for(n - 1, 256), 256, 0, s>>>(nodes, n - 1, sc.nsize, nodes4);
+    note_launches(1);
+  }
   return cudaGetLastError();
 }
 

@@ -44,6 +44,19 @@ struct __align__(16) Node {
   float4 a, b, c, d;
 };
 
+// BVH4 node, 128 bytes: the boxes of up to four children as structure of
+// arrays (lane j of each float4 is child j) and their references; missing
+// children have the reference kEmptyRef. Node i of the BVH4 array is BVH2 node
+// i with each internal child replaced by that child's two children, so the
+// internal children of a BVH4 node are BVH2 nodes two levels down and the
+// BVH4 array is indexed like the BVH2 array (odd-level entries are unused).
+struct __align__(16) Node4 {
+  float4 lox, hix, loy, hiy, loz, hiz;
+  int4 child;
+  int4 pad;
+};
+constexpr int kStackDepth4 = 96;  // 3 pushes per BVH4 level
+
 // Triangle record, 48 bytes: v0.xyz + original id, v1.xyz, v2.xyz.
 struct __align__(16) Tri {
   float4 v0, v1, v2;

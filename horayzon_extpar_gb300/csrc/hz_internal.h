@@ -71,10 +71,12 @@ size_t bvh_scratch_bytes(long long n_tri);
 // Builds nodes[n_tri - 1] (or one node when n_tri <= kLeafMax) and tris[n_tri];
 // the root is node 0. n_tri == 0 leaves the tree empty.
 // With vert_lo, also writes tri_lo[3 * n_tri]: the FP32 residuals of v0, v1,
-// v2 per triangle in leaf order (precise mode).
+// v2 per triangle in leaf order (precise mode). With nodes4 (same length as
+// nodes), also the BVH4 collapse of the tree (root 0).
 cudaError_t bvh_build(const float* vert32, const int* vot, int n_tri, Node* nodes,
                       Tri* tris, const BvhScratch& sc, cudaStream_t s,
-                      const float* vert_lo = nullptr, float4* tri_lo = nullptr);
+                      const float* vert_lo = nullptr, float4* tri_lo = nullptr,
+                      Node4* nodes4 = nullptr);
 
 // ---- hz_trace.cu ------------------------------------------------------------
 struct TraceParams {
@@ -123,6 +125,7 @@ cudaError_t cell_order(const double* cell_enu, int begin, int count, int id_offs
 struct DomainDesc {
   const double* cell_enu;     // [3 * ncell] FP64 ENU of cell centres
   const Node* nodes;
+  const Node4* nodes4;        // BVH4 collapse of nodes (wide traversal only)
   const Tri* tris;
   const float4* tri_lo;       // precise mode: [3 * n_tri] FP32 vertex residuals
   double* horizon;            // [nhori * ncell] degrees
@@ -145,9 +148,19 @@ struct DomainDesc {
 // `total` work ids from `order`; a work id is cell_offset + cell of its
 // domain, and `doms` is sorted by cell_offset.
 // precise: every domain carries tri_lo and rays use hi + lo vertices/origin.
+// variant: the BVH the search traverses (kTrace*); advance_min / leaf_min:
+// lanes of a warp that must be waiting before the search state advances /
+// holding a postponed leaf before a triangle pass runs.
+enum : int {
+  kTraceWide = 0,   // 4-wide BVH (DomainDesc::nodes4)
+  kTraceBinary = 1  // binary BVH (DomainDesc::nodes)
+};
+constexpr int kDefaultAdvanceMin = 16;
+constexpr int kDefaultLeafMin = 12;
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
                        int* work, unsigned long long* counters, int* err, int advance_min,
-                       bool count_work, bool precise, cudaStream_t s);
+                       int leaf_min, int variant, bool count_work, bool precise,
+                       cudaStream_t s);
 
 // ---- hz_learn.cu ------------------------------------------------------------
 constexpr int kMlpIn = 32;

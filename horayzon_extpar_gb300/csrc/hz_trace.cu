@@ -315,19 +315,35 @@ __global__ void __launch_bounds__(128) k_trace_exact(TraceParams p) {
 }
 
 // ---------------------------------------------------------------------------
-// Persistent, flattened variant. Same search and the same rays as
-// k_trace_exact, restructured for SIMT efficiency: every loop iteration runs
-// one traversal step (one BVH node or one leaf) for all lanes; a lane whose
-// ray has finished advances its cell's search state machine (next elevation,
-// next azimuth or next cell) only once at least `advance_min` lanes of the
-// warp are waiting, so the FP64 search code runs for many lanes at once.
-// Lanes take cells from a global counter in the order given by `order`
-// (Morton order of the cells), and keep their FP64 search state in shared
-// memory to leave registers to the traversal.
+// Persistent search (the TBB loop over cells, cpp:683-761, with its Embree
+// queries). Same search and the same rays as k_trace_exact, restructured for
+// the SIMT machine:
+//   * persistent blocks take cells from a global counter in the order given
+//     by `order` (Morton order of the cells); each lane owns one cell at a
+//     time and runs its bracketing search as a state machine;
+//   * every loop iteration is executed by all 32 lanes of a warp (the loop
+//     ends when no lane has work left), so the ballots see the whole warp;
+//   * a lane whose ray has finished advances its search (next elevation, next
+//     azimuth or next cell) only once at least `advance_min` lanes of the warp
+//     are waiting, so the FP64 search code runs for many lanes at once;
+//   * the traversal alternates node passes and triangle passes. A node pass
+//     visits one BVH node for every lane whose next target is a node; a leaf
+//     reached this way is postponed (one per lane) and the lane continues
+//     from its stack. A triangle pass runs when at least `leaf_min` lanes hold
+//     a postponed leaf, or when no lane has a node left to visit, and tests
+//     ONE triangle per such lane. Occlusion is an any-hit query, so the order
+//     in which leaves are tested changes no hit decision;
+//   * the search state (FP64 frame and sums, lattice index, azimuth, cell,
+//     FP32 origin) lives in shared memory; registers hold the ray and its
+//     traversal.
+// kWide: the 4-wide BVH (Node4); otherwise the binary BVH.
 // ---------------------------------------------------------------------------
 constexpr int kFlatBlock = 128;
+#ifndef HZ_WARP_MIN_BLOCKS
+#define HZ_WARP_MIN_BLOCKS 6  // resident blocks per SM the register budget targets
+#endif
 
-enum : int { kPhaseFirst = 0, kPhaseUp = 1, kPhaseDown = 2 };
+enum : int { kPhaseStart = 0, kPhaseFirst = 1, kPhaseUp = 2, kPhaseDown = 3 };
 
 // Visits internal node `ref`: descends into the nearer hit child (pushing the
 // other), or pops. Returns false on stack overflow.
@@ -357,62 +373,120 @@ __device__ __forceinline__ bool visit_node(const Node* __restrict__ nodes, const
   return true;
 }
 
-// Tests the triangles of leaf `ref`; true on the first hit. kPrecise: with
-// the FP32 residuals in tri_lo (hi + lo vertices, hi + lo origin).
-template <bool kCount, bool kPrecise>
-__device__ __forceinline__ bool test_leaf(const Tri* __restrict__ tris,
-                                          const float4* __restrict__ tri_lo, const Ray& r,
-                                          int ref, unsigned long long& ntest) {
-  const int s0 = leaf_start(ref), cnt = leaf_count(ref);
-  for (int k = s0; k < s0 + cnt; k++) {
-    if (kCount) ntest++;
-    const float4 v0 = __ldg(&tris[k].v0);
-    const float4 v1 = __ldg(&tris[k].v1);
-    const float4 v2 = __ldg(&tris[k].v2);
-    if (kPrecise) {
-      const float4 l0 = __ldg(&tri_lo[3LL * k]);
-      const float4 l1 = __ldg(&tri_lo[3LL * k + 1]);
-      const float4 l2 = __ldg(&tri_lo[3LL * k + 2]);
-      if (tri_hit_hl(r, v0, v1, v2, l0, l1, l2)) return true;
-    } else {
-      if (tri_hit(r, v0, v1, v2)) return true;
-    }
+// Visits BVH4 node `ref`: continues with the nearest hit child and pushes the
+// other hit children, farthest first; pops when no child is hit. Returns false
+// on stack overflow.
+__device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, const Ray& r,
+                                            int& ref, int* stack, int& sp) {
+  const Node4* nd = nodes4 + ref;
+  const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix);
+  const float4 ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
+  const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
+  const int4 ch = __ldg(&nd->child);
+  float t0, t1, t2, t3;
+  int r0 = ch.x, r1 = ch.y, r2 = ch.z, r3 = ch.w;
+  if (!(r0 != kEmptyRef && box_hit(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, t0))) t0 = INFINITY;
+  if (!(r1 != kEmptyRef && box_hit(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, t1))) t1 = INFINITY;
+  if (!(r2 != kEmptyRef && box_hit(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, t2))) t2 = INFINITY;
+  if (!(r3 != kEmptyRef && box_hit(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, t3))) t3 = INFINITY;
+  // Sorting network on (t, ref): (0,1) (2,3) (0,2) (1,3) (1,2).
+  auto cx = [](float& ta, int& ra, float& tb, int& rb) {
+    const bool sw = tb < ta;
+    const float t = sw ? tb : ta;
+    const int q = sw ? rb : ra;
+    tb = sw ? ta : tb;
+    rb = sw ? ra : rb;
+    ta = t;
+    ra = q;
+  };
+  cx(t0, r0, t1, r1);
+  cx(t2, r2, t3, r3);
+  cx(t0, r0, t2, r2);
+  cx(t1, r1, t3, r3);
+  cx(t1, r1, t2, r2);
+  if (t0 == INFINITY) {
+    ref = sp > 0 ? stack[--sp] : kEmptyRef;
+    return true;
   }
-  return false;
+  const int extra = (t1 != INFINITY) + (t2 != INFINITY) + (t3 != INFINITY);
+  if (sp + extra > kStackDepth4) return false;
+  if (t3 != INFINITY) stack[sp++] = r3;
+  if (t2 != INFINITY) stack[sp++] = r2;
+  if (t1 != INFINITY) stack[sp++] = r1;
+  ref = r0;
+  return true;
 }
 
-template <bool kCount, bool kPrecise>
-__global__ void __launch_bounds__(kFlatBlock, 8)
-    k_trace_flat(const DomainDesc* __restrict__ doms, int ndom, const int* __restrict__ order,
-                 int total, int* __restrict__ work, unsigned long long* __restrict__ counters,
-                 int* __restrict__ err, int advance_min) {
-  // Per-lane FP64 search state: 0-2 sphere normal U, 3-5 north N, 6-8 east E,
-  // 9-11 horizontal direction of the current azimuth, 12 elevation
-  // accumulator, 13 sector sum, 14 SVF sum.
-  __shared__ double sv[15][kFlatBlock];
-  const int t = threadIdx.x;
+// One ray/triangle test of triangle k (kPrecise: hi + lo vertices).
+template <bool kPrecise>
+__device__ __forceinline__ bool test_tri(const Tri* __restrict__ tris,
+                                         const float4* __restrict__ tri_lo, const Ray& r, int k) {
+  const float4 v0 = __ldg(&tris[k].v0);
+  const float4 v1 = __ldg(&tris[k].v1);
+  const float4 v2 = __ldg(&tris[k].v2);
+  if (kPrecise) {
+    const float4 l0 = __ldg(&tri_lo[3LL * k]);
+    const float4 l1 = __ldg(&tri_lo[3LL * k + 1]);
+    const float4 l2 = __ldg(&tri_lo[3LL * k + 2]);
+    return tri_hit_hl(r, v0, v1, v2, l0, l1, l2);
+  }
+  return tri_hit(r, v0, v1, v2);
+}
 
-  int dom = 0, cell = -1, a = 0, phase = kPhaseFirst, up = 0, m = 0;
-  bool need = true, start = true, last_hit = false;
+template <bool kCount, bool kPrecise, bool kWide>
+__global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
+    k_trace_warp(const DomainDesc* __restrict__ doms, int ndom, const int* __restrict__ order,
+                 int total, int* __restrict__ work, unsigned long long* __restrict__ counters,
+                 int* __restrict__ err, int advance_min, int leaf_min) {
+  // Per-lane search state. FP64: 0-2 sphere normal U, 3-5 north N, 6-8 east
+  // E, 9-11 horizontal direction of the current azimuth, 12 elevation
+  // accumulator, 13 sector sum, 14 SVF sum. Integers: domain, cell, azimuth,
+  // phase, upward steps, lattice index m of the current elevation. FP32 ray
+  // origin (hi, and lo in precise mode).
+  __shared__ double sv[15][kFlatBlock];
+  __shared__ int si[6][kFlatBlock];
+  __shared__ float so[6][kFlatBlock];
+  constexpr unsigned kFull = 0xffffffffu;
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int q = 0; q < 6; q++) si[q][t] = 0;
+  si[3][t] = kPhaseStart;
+
+  bool alive = true, need = true, last_hit = false;
   int ref = kEmptyRef, sp = 0;
-  int stack[kStackDepth];
+  int pst = 0, pcnt = 0;  // postponed leaf: next triangle, triangles left
+  int stack[kWide ? kStackDepth4 : kStackDepth];
   const Node* nodes = nullptr;
+  const Node4* nodes4 = nullptr;
   const Tri* tris = nullptr;
   const float4* tri_lo = nullptr;
-  int root = kEmptyRef;
-  float tfar = 0.f;
-  float ox = 0.f, oy = 0.f, oz = 0.f;
-  float olx = 0.f, oly = 0.f, olz = 0.f;
   Ray r;
   unsigned long long rays = 0, nvis = 0, ntest = 0;
 
+  // A leaf target becomes the postponed leaf when the lane holds none; a ray
+  // with neither a target nor a postponed leaf has missed.
+  auto settle = [&]() {
+    if (ref < 0 && ref != kEmptyRef && pcnt == 0) {
+      pst = leaf_start(ref);
+      pcnt = leaf_count(ref);
+      ref = sp > 0 ? stack[--sp] : kEmptyRef;
+    }
+    if (ref == kEmptyRef && pcnt == 0) {
+      need = true;
+      last_hit = false;
+    }
+  };
+
   for (;;) {
-    const unsigned act = __activemask();
-    const unsigned waiting = __ballot_sync(act, need);
-    if (need && (__popc(waiting) >= advance_min || waiting == act)) {
-      bool emit = false, alive = true;
+    const unsigned live = __ballot_sync(kFull, alive);
+    if (live == 0u) break;
+    const unsigned waiting = __ballot_sync(kFull, alive && need);
+    if (waiting != 0u && (__popc(waiting) >= advance_min || waiting == live) && alive && need) {
+      int dom = si[0][t], cell = si[1][t], a = si[2][t], phase = si[3][t], up = si[4][t];
+      int m = si[5][t];
+      bool emit = false;
       while (!emit) {
-        if (start) {
+        if (phase == kPhaseStart) {
           const int k = atomicAdd(work, 1);
           if (k >= total) {
             alive = false;
@@ -428,11 +502,6 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
           dom = lo;
           const DomainDesc& D = doms[dom];
           cell = (int)(g - D.cell_offset);
-          nodes = D.nodes;
-          tris = D.tris;
-          if (kPrecise) tri_lo = D.tri_lo;
-          root = D.root;
-          tfar = D.tfar;
           // Cell frame, mo_lradtopo_horayzon.cpp:694-720.
           const V3 q{D.cell_enu[3LL * cell], D.cell_enu[3LL * cell + 1],
                      D.cell_enu[3LL * cell + 2]};
@@ -446,13 +515,14 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
           const double o64x = q.x + normal.x * D.ray_org_elev;
           const double o64y = q.y + normal.y * D.ray_org_elev;
           const double o64z = q.z + normal.z * D.ray_org_elev;
-          ox = (float)o64x;
-          oy = (float)o64y;
-          oz = (float)o64z;
+          const float ox = (float)o64x, oy = (float)o64y, oz = (float)o64z;
+          so[0][t] = ox;
+          so[1][t] = oy;
+          so[2][t] = oz;
           if (kPrecise) {
-            olx = (float)(o64x - (double)ox);
-            oly = (float)(o64y - (double)oy);
-            olz = (float)(o64z - (double)oz);
+            so[3][t] = (float)(o64x - (double)ox);
+            so[4][t] = (float)(o64y - (double)oy);
+            so[5][t] = (float)(o64z - (double)oz);
           }
           sv[0][t] = normal.x; sv[1][t] = normal.y; sv[2][t] = normal.z;
           sv[3][t] = north.x; sv[4][t] = north.y; sv[5][t] = north.z;
@@ -461,7 +531,6 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
           a = 0;
           m = 0;
           phase = kPhaseFirst;
-          start = false;
         } else {
           // Result of the last ray: continue the bracket or close the azimuth.
           const DomainDesc& D = doms[dom];
@@ -515,7 +584,7 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
                 D.done[1] = now;
               }
             }
-            start = true;
+            phase = kPhaseStart;
             continue;
           }
           sv[13][t] = sector;
@@ -535,44 +604,72 @@ __global__ void __launch_bounds__(kFlatBlock, 8)
         sv[11][t] = cs.x * sv[5][t] + cs.y * sv[8][t];
         emit = true;
       }
-      if (!alive) break;
-      // Direction at lattice elevation m: cos(e_m) h_a + sin(e_m) U.
-      double2 ecs;
-      if (m >= kElevMin && m < kElevMin + kElevTable) {
-        ecs = __ldg(&doms[dom].elev_cs[m - kElevMin]);
-      } else {
-        const double e = (double)m * (2.0 * doms[dom].hori_acc);
-        ecs = make_double2(cos(e), sin(e));
+      si[3][t] = phase;
+      if (alive) {
+        si[0][t] = dom;
+        si[1][t] = cell;
+        si[2][t] = a;
+        si[4][t] = up;
+        si[5][t] = m;
+        const DomainDesc& D = doms[dom];
+        if (kWide) nodes4 = D.nodes4;
+        else nodes = D.nodes;
+        tris = D.tris;
+        if (kPrecise) tri_lo = D.tri_lo;
+        // Direction at lattice elevation m: cos(e_m) h_a + sin(e_m) U.
+        double2 ecs;
+        if (m >= kElevMin && m < kElevMin + kElevTable) {
+          ecs = __ldg(&D.elev_cs[m - kElevMin]);
+        } else {
+          const double e = (double)m * (2.0 * D.hori_acc);
+          ecs = make_double2(cos(e), sin(e));
+        }
+        const float dx = (float)(ecs.x * sv[9][t] + ecs.y * sv[0][t]);
+        const float dy = (float)(ecs.x * sv[10][t] + ecs.y * sv[1][t]);
+        const float dz = (float)(ecs.x * sv[11][t] + ecs.y * sv[2][t]);
+        if (kPrecise)
+          r = make_ray(so[0][t], so[1][t], so[2][t], dx, dy, dz, D.tfar, so[3][t], so[4][t],
+                       so[5][t]);
+        else
+          r = make_ray(so[0][t], so[1][t], so[2][t], dx, dy, dz, D.tfar);
+        ref = D.root;
+        sp = 0;
+        pcnt = 0;
+        need = false;
+        rays++;
+        settle();
       }
-      const float dx = (float)(ecs.x * sv[9][t] + ecs.y * sv[0][t]);
-      const float dy = (float)(ecs.x * sv[10][t] + ecs.y * sv[1][t]);
-      const float dz = (float)(ecs.x * sv[11][t] + ecs.y * sv[2][t]);
-      r = make_ray(ox, oy, oz, dx, dy, dz, tfar, olx, oly, olz);
-      ref = root;
-      sp = 0;
-      need = false;
-      rays++;
     }
-    if (need) continue;
 
-    // One traversal step: one internal node or one leaf.
-    bool fin = false, hit = false;
-    if (ref >= 0) {
+    // Node pass.
+    if (alive && !need && ref >= 0) {
       if (kCount) nvis++;
-      if (!visit_node(nodes, r, ref, stack, sp)) {
+      if (!(kWide ? visit_node4(nodes4, r, ref, stack, sp)
+                  : visit_node(nodes, r, ref, stack, sp))) {
         atomicOr(err, kErrStack);
-        fin = true;
-        hit = true;
+        need = true;
+        last_hit = true;
+      } else {
+        settle();
       }
-    } else if (ref != kEmptyRef) {
-      hit = test_leaf<kCount, kPrecise>(tris, tri_lo, r, ref, ntest);
-      if (hit) fin = true;
-      else ref = sp > 0 ? stack[--sp] : kEmptyRef;
     }
-    if (!fin && ref == kEmptyRef) fin = true;
-    if (fin) {
-      need = true;
-      last_hit = hit;
+    // Triangle pass.
+    const bool has_leaf = alive && !need && pcnt > 0;
+    const unsigned pend = __ballot_sync(kFull, has_leaf);
+    if (pend != 0u) {
+      const unsigned nodes_left = __ballot_sync(kFull, alive && !need && ref >= 0);
+      if ((__popc(pend) >= leaf_min || nodes_left == 0u) && has_leaf) {
+        if (kCount) ntest++;
+        const bool hit = test_tri<kPrecise>(tris, tri_lo, r, pst);
+        pst++;
+        pcnt--;
+        if (hit) {
+          need = true;
+          last_hit = true;
+        } else if (pcnt == 0) {
+          settle();
+        }
+      }
     }
   }
   rays = warp_sum_u64(rays);
@@ -700,37 +797,47 @@ cudaError_t cell_order(const double* cell_enu, int begin, int count, int id_offs
   return radix_sort_pairs(keys, order, keys_alt, vals_alt, count, 32, sort_scratch, s);
 }
 
-template <bool kCount, bool kPrecise>
-cudaError_t launch_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
-                        int* work, unsigned long long* counters, int* err, int advance_min,
-                        cudaStream_t s) {
+// One persistent launch: as many blocks as fit on the device at once, at
+// most one block per kFlatBlock work items.
+template <typename... P, typename... A>
+cudaError_t launch_persistent(void (*kernel)(P...), int total, cudaStream_t s, A... args) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_flat<kCount, kPrecise>,
-                                                kFlatBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kFlatBlock, 0);
   long long blocks = (long long)sms * (per_sm > 0 ? per_sm : 1);
   const long long needed = ((long long)total + kFlatBlock - 1) / kFlatBlock;
   if (blocks > needed) blocks = needed;
-  k_trace_flat<kCount, kPrecise><<<(unsigned)blocks, kFlatBlock, 0, s>>>(
-      doms, ndom, order, total, work, counters, err, advance_min);
+  kernel<<<(unsigned)blocks, kFlatBlock, 0, s>>>(args...);
   note_launches(1);
   return cudaGetLastError();
 }
 
+template <bool kCount, bool kPrecise>
+cudaError_t launch_variant(const DomainDesc* doms, int ndom, const int32_t* order, int total,
+                           int* work, unsigned long long* counters, int* err, int advance_min,
+                           int leaf_min, int variant, cudaStream_t s) {
+  if (variant == kTraceWide)
+    return launch_persistent(k_trace_warp<kCount, kPrecise, true>, total, s, doms, ndom, order,
+                             total, work, counters, err, advance_min, leaf_min);
+  return launch_persistent(k_trace_warp<kCount, kPrecise, false>, total, s, doms, ndom, order,
+                           total, work, counters, err, advance_min, leaf_min);
+}
+
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
                        int* work, unsigned long long* counters, int* err, int advance_min,
-                       bool count_work, bool precise, cudaStream_t s) {
+                       int leaf_min, int variant, bool count_work, bool precise,
+                       cudaStream_t s) {
   if (total <= 0 || ndom <= 0) return cudaSuccess;
   if (precise)
-    return count_work ? launch_flat<true, true>(doms, ndom, order, total, work, counters, err,
-                                                advance_min, s)
-                      : launch_flat<false, true>(doms, ndom, order, total, work, counters, err,
-                                                 advance_min, s);
-  return count_work ? launch_flat<true, false>(doms, ndom, order, total, work, counters, err,
-                                               advance_min, s)
-                    : launch_flat<false, false>(doms, ndom, order, total, work, counters, err,
-                                                advance_min, s);
+    return count_work ? launch_variant<true, true>(doms, ndom, order, total, work, counters,
+                                                   err, advance_min, leaf_min, variant, s)
+                      : launch_variant<false, true>(doms, ndom, order, total, work, counters,
+                                                    err, advance_min, leaf_min, variant, s);
+  return count_work ? launch_variant<true, false>(doms, ndom, order, total, work, counters, err,
+                                                  advance_min, leaf_min, variant, s)
+                    : launch_variant<false, false>(doms, ndom, order, total, work, counters,
+                                                   err, advance_min, leaf_min, variant, s);
 }
 
 cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s) {

@@ -8,7 +8,8 @@ the proposal and refines it exactly as without the MLP.
 
 Training data come from the plain method itself on other terrain seeds: the
 device entry point returns the features and the unclipped horizon lattice
-index of every (cell, azimuth) (hz_options.features / raw_index). Training
+index of every (cell, azimuth) (hz_options.features / raw_index); the
+targets are that index clipped below at -4 deg. Training
 runs on the GPU with the library's own forward, backward and Adam kernels
 (hz_mlp_train_step).
 """
@@ -24,6 +25,7 @@ from .horizon_svf import horizon_svf_comp_device
 
 N_IN = 32
 N_HID = 64
+TARGET_MIN_J = -16  # -4 deg in quarter degrees
 
 
 def num_params() -> int:
@@ -52,7 +54,10 @@ def training_samples(domain, args, max_samples: int | None = None, seed: int = 0
     feats = torch.empty((L, domain.ncell, N_IN), dtype=torch.float32, device=dev)
     horizon_svf_comp_device(*t, *args, raw_index=raw, features=feats)
     X = feats.reshape(-1, N_IN)
-    Y = raw.reshape(-1).to(torch.float32) / 32.0
+    # Horizons below -4 deg are clipped: the search reaches them by walking
+    # down from any start near 0 deg, and the few -85 deg "void" directions at
+    # the domain border would otherwise dominate the squared error.
+    Y = raw.reshape(-1).to(torch.float32).clamp_(min=TARGET_MIN_J) / 32.0
     if max_samples is not None and X.shape[0] > max_samples:
         g = torch.Generator(device=dev)
         g.manual_seed(seed)

@@ -69,6 +69,9 @@ typedef struct hz_options {
        num_hori * refine_factor. NULL = not written. */
     int16_t* raw_index;
     float* features;
+    int32_t leaf_min;        /* persistent kernel: lanes of a warp that must hold a
+                                postponed leaf before a triangle pass (1..32; 0 =
+                                library default) */
 } hz_options;
 
 enum {
@@ -84,8 +87,13 @@ enum {
 };
 
 enum {
-    HZ_KERNEL_PERSISTENT = 0,  /* flattened persistent search, Morton-ordered cells */
-    HZ_KERNEL_PER_CELL = 1     /* one thread per cell, nested loops */
+    HZ_KERNEL_PERSISTENT = 0,  /* persistent search over Morton-ordered cells on a 4-wide
+                                  BVH, warp-uniform loop, postponed leaves tested one
+                                  triangle per pass */
+    HZ_KERNEL_PER_CELL = 1,    /* one thread per cell, nested loops, binary BVH */
+    HZ_KERNEL_PERSISTENT_BVH2 = 2  /* the persistent search on the binary BVH (same rays
+                                      and results; its node visits are the binary-tree
+                                      counts) */
 };
 
 typedef struct hz_stats {

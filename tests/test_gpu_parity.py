@@ -188,16 +188,19 @@ def test_gpu_dropin_c_symbol(small_domain):
     np.testing.assert_array_equal(s, so)
 
 
-@pytest.mark.parametrize("kernel,advance_min", [(0, 1), (0, 4), (0, 16), (0, 32)])
-def test_gpu_persistent_equals_per_cell(small_domain, kernel, advance_min):
-    """The persistent search (closed-form lattice directions) casts the same
-    rays as the per-cell search (the reference's incremental rotations)."""
+@pytest.mark.parametrize("kernel,advance_min,leaf_min",
+                         [(0, 1, 1), (0, 4, 32), (0, 16, 8), (0, 32, 16), (0, 0, 0),
+                          (2, 1, 32), (2, 24, 4), (2, 0, 0)])
+def test_gpu_persistent_equals_per_cell(small_domain, kernel, advance_min, leaf_min):
+    """The persistent searches (closed-form lattice directions; any leaf
+    order) cast the same rays as the per-cell search (the reference's
+    incremental rotations)."""
     args = (24, 1, 40000.0, 0.2, 1, 2)
     h1, s1, st1 = horizon_svf_comp_py(*small_domain.inputs(), *args, kernel=1,
                                       count_work=True, return_stats=True)
     h2, s2, st2 = horizon_svf_comp_py(*small_domain.inputs(), *args, kernel=kernel,
-                                      advance_min=advance_min, count_work=True,
-                                      return_stats=True)
+                                      advance_min=advance_min, leaf_min=leaf_min,
+                                      count_work=True, return_stats=True)
     np.testing.assert_array_equal(h1, h2)
     # SVF: tabulated sin of the lattice angle vs sin of the accumulated angle
     np.testing.assert_allclose(s1, s2, rtol=0, atol=1e-12)
