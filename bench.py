@@ -366,15 +366,17 @@ def run_gpu(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def step(count=False, kernel=_lib.HZ_KERNEL_PERSISTENT):
+    def step(count=False, kernel=_lib.HZ_KERNEL_PERSISTENT, leaf_size=0):
         return horizon_svf_comp_device(*d_in, *ARGS, horizon=horizon, skyview=skyview,
-                                       stream=stream, count_work=count, kernel=kernel)[2]
+                                       stream=stream, count_work=count, kernel=kernel,
+                                       leaf_size=leaf_size)[2]
 
     # Untimed: work counters. The algorithmic bytes are defined on the binary
-    # LBVH (64 B per node visit, 48 B per triangle test), so they are counted
-    # by the same search on the BVH2; the 4-wide counts of the timed kernel
-    # are reported beside them.
-    st_count = step(count=True, kernel=_lib.HZ_KERNEL_PERSISTENT_BVH2)
+    # LBVH with leaves of <= 4 triangles (64 B per node visit, 48 B per
+    # triangle test), so they are counted by the same search on that tree;
+    # the counts of the timed kernel (4-wide tree, default leaves) are
+    # reported beside them.
+    st_count = step(count=True, kernel=_lib.HZ_KERNEL_PERSISTENT_BVH2, leaf_size=4)
     st_wide = step(count=True)
     l2_peak = l2_read_peak(dev)
     for _ in range(args.warmup):

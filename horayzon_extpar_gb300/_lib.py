@@ -19,7 +19,8 @@ _I = C.POINTER(C.c_int32)
 HZ_OK, HZ_ERR_VALUE, HZ_ERR_TYPE, HZ_ERR_INDEX, HZ_ERR_CUDA, HZ_ERR_INTERNAL = range(6)
 
 #: Every symbol include/horayzon_gb300.h declares.
-EXPORTED_SYMBOLS = ("hz_default_options", "horizon_svf_comp", "hz_horizon_svf",
+EXPORTED_SYMBOLS = ("hz_default_options", "horizon_svf_comp", "horizon_svf_comp_buffer",
+                    "hz_horizon_svf",
                     "hz_horizon_svf_device", "hz_build_mesh", "hz_mesh_enu32",
                     "hz_last_error", "hz_version", "hz_release_workspace",
                     "hz_horizon_svf_device_static", "hz_horizon_svf_batch",
@@ -45,7 +46,8 @@ class Options(C.Structure):
                 ("kernel", C.c_int32), ("advance_min", C.c_int32),
                 ("precision", C.c_int32), ("mlp_params", C.c_void_p),
                 ("mlp_every_azimuth", C.c_int32), ("raw_index", C.c_void_p),
-                ("features", C.c_void_p), ("leaf_min", C.c_int32)]
+                ("features", C.c_void_p), ("leaf_min", C.c_int32),
+                ("leaf_size", C.c_int32)]
 
 
 HZ_KERNEL_PERSISTENT, HZ_KERNEL_PER_CELL, HZ_KERNEL_PERSISTENT_BVH2 = 0, 1, 2
@@ -104,6 +106,9 @@ def load(build_if_missing: bool = True):
                   C.c_int]
         L.horizon_svf_comp.restype = None
         L.horizon_svf_comp.argtypes = [_D, _D, _D, _D, _D, _I, _D, _D] + common
+        L.horizon_svf_comp_buffer.restype = None
+        L.horizon_svf_comp_buffer.argtypes = ([_D, _D, _D, _D, _D, _I, _D, _D] + common +
+                                              [C.c_char_p, C.POINTER(C.c_int)])
         L.hz_horizon_svf.restype = C.c_int
         L.hz_horizon_svf.argtypes = ([_D, _D, _D, _D, _D, _I, _D, _D] + common +
                                      [C.POINTER(Options), C.POINTER(Stats)])

@@ -28,6 +28,19 @@ namespace {
 
 thread_local std::string g_last_error;
 thread_local long long g_launches = 0;
+// Progress lines of the current call (the reference's std::cout lines).
+thread_local std::string g_log;
+
+void log_line(const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_log += buf;
+}
+const char* kRule =
+    "-------------------------------------------------------------------------------\n";
 
 int fail(int code, const char* fmt, ...) {
   char buf[512];
@@ -195,7 +208,7 @@ BatchBuffers carve_batch(Carver& c, int n, long long total_cells) {
   b.doms = c.take<DomainDesc>(n);
   b.order = c.take<int32_t>(total_cells);
   b.work = c.take<int>(4);
-  b.counters = c.take<unsigned long long>(4);
+  b.counters = c.take<unsigned long long>(kCounterWords);
   b.done = c.take<unsigned long long>(2 * (size_t)n);
   b.t0 = c.take<unsigned long long>(2);
   b.err = c.take<int>(4);
@@ -346,6 +359,7 @@ enum class Stop { kMesh, kEnu, kFull };
 struct RunOut {
   std::vector<int> n_tri, n_mv;
   std::vector<double> latency_ms;
+  std::vector<double> origin_lat, origin_lon;  // ENU origin per domain [deg]
 };
 
 // Runs the pipeline for n domains whose arrays are device pointers in pr[].
@@ -354,9 +368,12 @@ struct RunOut {
 int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const BatchBuffers& bb,
               cudaStream_t s, const hz_options& opt, hz_stats* st, Stop stop, RunOut* out) {
   g_launches = 0;
+  g_log.clear();
   out->n_tri.assign(n, 0);
   out->n_mv.assign(n, 0);
   out->latency_ms.assign(n, 0.0);
+  out->origin_lat.assign(n, 0.0);
+  out->origin_lon.assign(n, 0.0);
   // Pinned layout (64-bit words): 0-63 counters and flags; 64 + [0, n) mesh
   // totals; 64 + [n, 2n) error words; 64 + [2n, 5n) cell ECEF sums; the
   // search descriptors from word 64 + 5n + 8.
@@ -366,7 +383,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   unsigned long long* pin = E.pinned;
   for (int d = 0; d < n; d++) HZ_CUDA(cudaMemsetAsync(b[d].err, 0, 4 * sizeof(int), s));
   HZ_CUDA(cudaMemsetAsync(bb.err, 0, 4 * sizeof(int), s));
-  HZ_CUDA(cudaMemsetAsync(bb.counters, 0, 4 * sizeof(unsigned long long), s));
+  HZ_CUDA(cudaMemsetAsync(bb.counters, 0, kCounterWords * sizeof(unsigned long long), s));
   HZ_CUDA(cudaMemsetAsync(bb.done, 0, 2 * sizeof(unsigned long long) * (size_t)n, s));
   HZ_CUDA(cudaEventRecord(E.ev[0], s));
 
@@ -394,12 +411,6 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     out->n_tri[d] = (int)(tot & 0xFFFFFFFFull);
     nadd[d] = (int)(tot >> 32);
     out->n_mv[d] = pr[d].ncell + nadd[d];
-    if (opt.verbose) {
-      printf("Build triangle mesh from ICON grid cell circumcenters%s\n",
-             pr[d].grid_type == 0 ? "\n (non-unique triangulation)"
-                                  : " and vertices\n (unique triangulation)");
-      printf("Number of triangles in mesh: %d\n", out->n_tri[d]);
-    }
   }
   for (int d = 0; d < n; d++) {
     const Problem& P = pr[d];
@@ -423,12 +434,10 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   std::vector<Frame> frames(n);
   for (int d = 0; d < n; d++) {
     frames[d] = make_frame(sums[3 * d], sums[3 * d + 1], sums[3 * d + 2]);
-    if (opt.verbose) {
-      const double* so = sums + 3 * d;
-      const double radius = sqrt(so[0] * so[0] + so[1] * so[1] + so[2] * so[2]);
-      printf("Origin of ENU coordinate system: %.4f deg lat, %.4f deg lon\n",
-             rad2deg(asin(so[2] / radius)), rad2deg(atan2(so[1], so[0])));
-    }
+    const double* so = sums + 3 * d;
+    const double radius = sqrt(so[0] * so[0] + so[1] * so[1] + so[2] * so[2]);
+    out->origin_lat[d] = rad2deg(asin(so[2] / radius));
+    out->origin_lon[d] = rad2deg(atan2(so[1], so[0]));
     HZ_CUDA(mesh_enu(b[d].ecef, out->n_mv[d], pr[d].ncell, frames[d], b[d].vert32,
                      b[d].cell_enu, b[d].vert_lo, s));
   }
@@ -438,7 +447,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   // ---- BVH (cpp:395-432) ----
   for (int d = 0; d < n; d++)
     HZ_CUDA(bvh_build(b[d].vert32, b[d].vot, out->n_tri[d], b[d].nodes, b[d].tris, b[d].bvh, s,
-                      b[d].vert_lo, b[d].tri_lo, b[d].nodes4));
+                      b[d].vert_lo, b[d].tri_lo, b[d].nodes4, opt.leaf_size));
   HZ_CUDA(cudaEventRecord(E.ev[2], s));
 
   // ---- horizon + SVF (cpp:651-761) ----
@@ -617,7 +626,16 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   if (n > 1)
     HZ_CUDA(cudaMemcpyAsync(rb_done, bb.done, 2 * sizeof(unsigned long long) * (size_t)n,
                             cudaMemcpyDeviceToHost, s));
+#ifdef HZ_DIAG
+  HZ_CUDA(cudaMemcpyAsync(rb + 32, bb.counters, kCounterWords * sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, s));
+#endif
   HZ_CUDA(cudaStreamSynchronize(s));
+#ifdef HZ_DIAG
+  fprintf(stderr, "hz_diag");
+  for (int k = 0; k < kCounterWords; k++) fprintf(stderr, " %llu", rb[32 + k]);
+  fprintf(stderr, "\n");
+#endif
   const int err1 = (int)(rb[12] & 0xFFFFFFFFull);
   if (err1 & kErrStack) return fail(HZ_ERR_INTERNAL, "BVH traversal stack overflow");
   if (n > 1)
@@ -645,16 +663,42 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     cudaEventElapsedTime(&ms, E.ev[2], E.ev[3]);
     st->ms_trace = ms;
   }
-  if (opt.verbose) {
-    long long cells = 0, evals = 0;
-    for (int d = 0; d < n; d++) {
-      cells += pr[d].cell_count;
-      evals += (long long)pr[d].cell_count * pr[d].nhori;
-    }
-    printf("Number of rays shot: %lld\n", (long long)rb[8]);
-    printf("Average number of rays per cell and azimuth sector: %.2f\n",
+  // Progress lines in the reference's order and wording (cpp:240-241,
+  // 278-279, 315, 427-428, 589-594, 606-608, 639-641, 671-680, 765-776), with
+  // the GPU phase times.
+  float ms_mesh = 0.f, ms_bvh = 0.f, ms_ray = 0.f;
+  cudaEventElapsedTime(&ms_mesh, E.ev[0], E.ev[1]);
+  cudaEventElapsedTime(&ms_bvh, E.ev[1], E.ev[2]);
+  cudaEventElapsedTime(&ms_ray, E.ev[2], E.ev[3]);
+  g_log += kRule;
+  log_line("Horizon and SVF computation on the GPU (horayzon_gb300 %d.%d.%d)\n",
+           HZ_VERSION / 100, (HZ_VERSION / 10) % 10, HZ_VERSION % 10);
+  g_log += kRule;
+  long long evals = 0;
+  for (int d = 0; d < n; d++) {
+    if (n > 1) log_line("Domain %d of %d\n", d + 1, n);
+    log_line("Build triangle mesh %s\n",
+             pr[d].grid_type == 0
+                 ? "solely from ICON grid cell circumcenters\n (non-unique triangulation)"
+                 : "from ICON grid cell circumcenters and vertices\n (unique triangulation)");
+    log_line("Number of triangles in mesh: %d\n", out->n_tri[d]);
+    if (d == 0) log_line("Triangle mesh building: %.2f s\n", 1e-3 * ms_mesh);
+    log_line("Origin of ENU coordinate system: %.4f deg lat, %.4f deg lon\n",
+             out->origin_lat[d], out->origin_lon[d]);
+    if (d == 0) log_line("Building bounding volume hierarchy (BVH): %.2f s\n", 1e-3 * ms_bvh);
+    static const char* kSvf[3] = {"pure geometric SVF", "geometric scaled with sin(horizon)",
+                                  "geometric scaled with sin(horizon)**2"};
+    log_line("Sky View Factor computation algorithm: %s\n", kSvf[pr[d].svf_type]);
+    evals += (long long)pr[d].cell_count * pr[d].nhori;
+  }
+  log_line("Ray tracing: %.2f s\n", 1e-3 * ms_ray);
+  log_line("Number of rays shot: %lld\n", (long long)rb[8]);
+  log_line("Average number of rays per cell and azimuth sector: %.2f\n",
            (double)rb[8] / (double)(evals > 0 ? evals : 1));
-    (void)cells;
+  g_log += kRule;
+  if (opt.verbose) {
+    fputs(g_log.c_str(), stdout);
+    fflush(stdout);
   }
   return HZ_OK;
 }
@@ -971,6 +1015,35 @@ void horizon_svf_comp(double* clon, double* clat, double* hsurf, double* vlon, d
       for (long long k = 0; k < (long long)num_hori * num_cell; k++) horizon[k] = NAN;
       for (int k = 0; k < num_cell; k++) skyview[k] = NAN;
     }
+  }
+}
+
+void horizon_svf_comp_buffer(double* clon, double* clat, double* hsurf, double* vlon,
+                             double* vlat, int* cells_of_vertex, double* horizon,
+                             double* skyview, int num_cell, int num_vertex, int num_hori,
+                             int grid_type, double dist_search, double ray_org_elev,
+                             int refine_factor, int svf_type, char* buffer, int* buffer_len) {
+  hz_options opt;
+  hz_default_options(&opt);
+  g_log.clear();
+  int rc = hz_horizon_svf(clon, clat, hsurf, vlon, vlat, cells_of_vertex, horizon, skyview,
+                          num_cell, num_vertex, num_hori, grid_type, dist_search,
+                          ray_org_elev, refine_factor, svf_type, &opt, nullptr);
+  if (rc != HZ_OK) {
+    g_log += "horizon_svf_comp: ";
+    g_log += hz_last_error();
+    g_log += "\n";
+    if (horizon && skyview && num_cell > 0 && num_hori > 0) {
+      for (long long k = 0; k < (long long)num_hori * num_cell; k++) horizon[k] = NAN;
+      for (int k = 0; k < num_cell; k++) skyview[k] = NAN;
+    }
+  }
+  // cpp:778-784: copy min(*buffer_len, length) bytes, no terminator, and
+  // return the count in *buffer_len.
+  if (buffer && buffer_len) {
+    const int n = std::max(0, std::min(*buffer_len, (int)g_log.size()));
+    if (n > 0) std::memcpy(buffer, g_log.data(), (size_t)n);
+    *buffer_len = n;
   }
 }
 

@@ -7,7 +7,8 @@
 //      plane (the terrain is a height field, so x/y carry the locality);
 //   3. stable radix sort of (key, triangle) pairs;
 //   4. k_karras: binary radix tree (Karras, HPG 2012) with index tie-break;
-//      subtrees of <= kLeafMax triangles become leaves;
+//      subtrees of <= leaf_max triangles (1..8, default kLeafMax) become
+//      leaves;
 //   5. k_gather: 48-byte triangle records in leaf order;
 //   6. k_refit: bottom-up boxes with one atomic arrival counter per node;
 //   7. optionally k_collapse4: the 4-wide tree used by the wide traversal.
@@ -105,7 +106,7 @@ __device__ __forceinline__ int delta(const uint32_t* __restrict__ keys, int n, i
 
 __global__ void k_karras(const uint32_t* __restrict__ keys, int n, Node* __restrict__ nodes,
                          int* __restrict__ parent, int* __restrict__ nsize,
-                         int* __restrict__ counter) {
+                         int* __restrict__ counter, int leaf_max) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1) return;
   const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -125,12 +126,12 @@ __global__ void k_karras(const uint32_t* __restrict__ keys, int n, Node* __restr
   const int gamma = i + s * d + (d < 0 ? d : 0);
   const int first = min(i, j), last = max(i, j);
   const int nl = gamma - first + 1, nr = last - gamma;
-  const int c0 = nl <= kLeafMax ? leaf_ref(first, nl) : gamma;
-  const int c1 = nr <= kLeafMax ? leaf_ref(gamma + 1, nr) : gamma + 1;
+  const int c0 = nl <= leaf_max ? leaf_ref(first, nl) : gamma;
+  const int c1 = nr <= leaf_max ? leaf_ref(gamma + 1, nr) : gamma + 1;
   nsize[i] = last - first + 1;
   counter[i] = 0;
   nodes[i].d = make_float4(__int_as_float(c0), __int_as_float(c1), 0.f, 0.f);
-  if (last - first + 1 > kLeafMax) {  // live node: its internal children are live
+  if (last - first + 1 > leaf_max) {  // live node: its internal children are live
     if (c0 >= 0) parent[c0] = (i << 1) | 0;
     if (c1 >= 0) parent[c1] = (i << 1) | 1;
   }
@@ -204,9 +205,10 @@ __device__ __forceinline__ Box union_of_children(const Node* node) {
 
 __global__ void k_refit(Node* __restrict__ nodes, const Tri* __restrict__ tris, int n,
                         const int* __restrict__ parent, const int* __restrict__ nsize,
-                        int* __restrict__ counter, const unsigned* __restrict__ bounds) {
+                        int* __restrict__ counter, const unsigned* __restrict__ bounds,
+                        int leaf_max) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n - 1 || nsize[i] <= kLeafMax) return;
+  if (i >= n - 1 || nsize[i] <= leaf_max) return;
   const float pad = __fmul_rn(ord2f(bounds[4]), 9.5367431640625e-07f);
   const float4 d = nodes[i].d;
   const int c0 = __float_as_int(d.x), c1 = __float_as_int(d.y);
@@ -230,7 +232,7 @@ __global__ void k_refit(Node* __restrict__ nodes, const Tri* __restrict__ tris, 
   }
 }
 
-// n_tri <= kLeafMax: one node, child 0 = leaf of all triangles, child 1 empty.
+// n_tri <= leaf_max: one node, child 0 = leaf of all triangles, child 1 empty.
 __global__ void k_small_root(Node* nodes, const Tri* __restrict__ tris, int n,
                              const unsigned* __restrict__ bounds) {
   const float pad = __fmul_rn(ord2f(bounds[4]), 9.5367431640625e-07f);
@@ -245,12 +247,13 @@ __global__ void k_small_root(Node* nodes, const Tri* __restrict__ tris, int n,
 
 // BVH4 node i from BVH2 node i: a leaf child stays, an internal child is
 // replaced by its two children (with the boxes that child stores for them).
-// Only live BVH2 nodes (ranges of more than kLeafMax triangles, or the single
+// Only live BVH2 nodes (ranges of more than leaf_max triangles, or the single
 // root of a small tree) are converted.
 __global__ void k_collapse4(const Node* __restrict__ nodes, int n_nodes,
-                            const int* __restrict__ nsize, Node4* __restrict__ out) {
+                            const int* __restrict__ nsize, int leaf_max,
+                            Node4* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_nodes || (nsize && nsize[i] <= kLeafMax)) return;
+  if (i >= n_nodes || (nsize && nsize[i] <= leaf_max)) return;
   float lo[3][4], hi[3][4];
   int ch[4];
   int k = 0;
@@ -304,7 +307,8 @@ size_t bvh_scratch_bytes(long long n) {
 
 cudaError_t bvh_build(const float* vert32, const int* vot, int n, Node* nodes, Tri* tris,
                       const BvhScratch& sc, cudaStream_t s, const float* vert_lo,
-                      float4* tri_lo, Node4* nodes4) {
+                      float4* tri_lo, Node4* nodes4, int leaf_max) {
+  if (leaf_max < 1 || leaf_max > 8) leaf_max = kLeafMax;
   if (n <= 0) return cudaSuccess;
   k_init_bounds<<<1, 1, 0, s>>>(sc.bounds);
   k_tri_bounds<<<grid_for(n, 256), 256, 0, s>>>(vert32, vot, n, sc.cxy, sc.bounds);
@@ -315,22 +319,23 @@ cudaError_t bvh_build(const float* vert32, const int* vot, int n, Node* nodes, T
   if (e != cudaSuccess) return e;
   k_gather<<<grid_for(n, 256), 256, 0, s>>>(vert32, vot, sc.vals, n, tris, vert_lo,
                                             vert_lo ? tri_lo : nullptr);
-  if (n <= kLeafMax) {
+  if (n <= leaf_max) {
     k_small_root<<<1, 1, 0, s>>>(nodes, tris, n, sc.bounds);
     note_launches(2);
     if (nodes4) {
-      k_collapse4<<<1, 32, 0, s>>>(nodes, 1, nullptr, nodes4);
+      k_collapse4<<<1, 32, 0, s>>>(nodes, 1, nullptr, leaf_max, nodes4);
       note_launches(1);
     }
     return cudaGetLastError();
   }
   note_launches(3);
   k_karras<<<grid_for(n - 1, 256), 256, 0, s>>>(sc.keys, n, nodes, sc.parent, sc.nsize,
-                                                sc.counter);
+                                                sc.counter, leaf_max);
   k_refit<<<grid_for(n - 1, 256), 256, 0, s>>>(nodes, tris, n, sc.parent, sc.nsize,
-                                               sc.counter, sc.bounds);
+                                               sc.counter, sc.bounds, leaf_max);
   if (nodes4) {
-    k_collapse4<<<grid_for(n - 1, 256), 256, 0, s>>>(nodes, n - 1, sc.nsize, nodes4);
+    k_collapse4<<<grid_for(n - 1, 256), 256, 0, s>>>(nodes, n - 1, sc.nsize, leaf_max,
+                                                     nodes4);
     note_launches(1);
   }
   return cudaGetLastError();

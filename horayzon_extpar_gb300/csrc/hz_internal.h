@@ -68,7 +68,8 @@ struct BvhScratch {
   void* sort_scratch;   // radix_scratch_u32(n)
 };
 size_t bvh_scratch_bytes(long long n_tri);
-// Builds nodes[n_tri - 1] (or one node when n_tri <= kLeafMax) and tris[n_tri];
+// Builds nodes[n_tri - 1] (or one node when n_tri <= leaf_max) and tris[n_tri];
+// leaves hold at most leaf_max triangles (1..8; other values: kLeafMax);
 // the root is node 0. n_tri == 0 leaves the tree empty.
 // With vert_lo, also writes tri_lo[3 * n_tri]: the FP32 residuals of v0, v1,
 // v2 per triangle in leaf order (precise mode). With nodes4 (same length as
@@ -76,7 +77,7 @@ size_t bvh_scratch_bytes(long long n_tri);
 cudaError_t bvh_build(const float* vert32, const int* vot, int n_tri, Node* nodes,
                       Tri* tris, const BvhScratch& sc, cudaStream_t s,
                       const float* vert_lo = nullptr, float4* tri_lo = nullptr,
-                      Node4* nodes4 = nullptr);
+                      Node4* nodes4 = nullptr, int leaf_max = kLeafMax);
 
 // ---- hz_trace.cu ------------------------------------------------------------
 struct TraceParams {
@@ -155,6 +156,9 @@ enum : int {
   kTraceWide = 0,   // 4-wide BVH (DomainDesc::nodes4)
   kTraceBinary = 1  // binary BVH (DomainDesc::nodes)
 };
+// Counter words of the search: 0 rays, 1 node visits, 2 triangle tests; with
+// -DHZ_DIAG, 3.. per-warp loop statistics (printed to stderr by the host).
+constexpr int kCounterWords = 16;
 constexpr int kDefaultAdvanceMin = 16;
 constexpr int kDefaultLeafMin = 12;
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,

@@ -125,7 +125,7 @@ StaticBuffers lay_out(Layout& L, long long ncell, long long nvert, long long max
   b.elev_cs = L.take<double2>(kElevTable);
   b.sin_lattice = L.take<double>(kSinTable);
   b.dom = L.take<DomainDesc>(1);
-  b.counters = L.take<unsigned long long>(4);
+  b.counters = L.take<unsigned long long>(kCounterWords);
   b.err = L.take<int>(4);
   return b;
 }
@@ -220,7 +220,7 @@ extern "C" int hz_horizon_svf_device_static(
 
   // Cleared every call: the array keeps the previous call's contents.
   HZ_STATIC_CUDA(cudaMemsetAsync(b.err, 0, 4 * sizeof(int), s), "clearing error word");
-  HZ_STATIC_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(unsigned long long), s),
+  HZ_STATIC_CUDA(cudaMemsetAsync(b.counters, 0, kCounterWords * sizeof(unsigned long long), s),
                  "clearing counters");
 
   // Mesh (mo_lradtopo_horayzon.cpp:228-317).

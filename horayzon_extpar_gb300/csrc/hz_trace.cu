@@ -29,6 +29,7 @@ struct Ray {
   float plx, ply, plz;    // precise mode: FP32 residual of the origin, permuted
   float Sx, Sy, Sz;       // shear constants
   int kx, ky, kz;
+  int nx, ny, nz;         // 1 where the inverse direction is negative (near plane = hi)
   float tfar;
 };
 
@@ -43,6 +44,9 @@ __device__ __forceinline__ Ray make_ray(float ox, float oy, float oz, float dx, 
   r.ox = ox; r.oy = oy; r.oz = oz;
   r.ix = __frcp_rn(dx); r.iy = __frcp_rn(dy); r.iz = __frcp_rn(dz);
   r.oix = __fmul_rn(ox, r.ix); r.oiy = __fmul_rn(oy, r.iy); r.oiz = __fmul_rn(oz, r.iz);
+  r.nx = signbit(r.ix) ? 1 : 0;
+  r.ny = signbit(r.iy) ? 1 : 0;
+  r.nz = signbit(r.iz) ? 1 : 0;
   const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
   int kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
   int kx = kz + 1 == 3 ? 0 : kz + 1;
@@ -143,16 +147,28 @@ __device__ __forceinline__ bool tri_hit_hl(const Ray& r, const float4 v0, const 
 
 // Conservative slab test: the boxes carry a margin far above the rounding of
 // these multiply-adds, so no triangle the watertight test would hit is culled.
-__device__ __forceinline__ bool box_hit(const Ray& r, float lx, float hx, float ly, float hy,
-                                        float lz, float hz, float& tentry) {
-  const float tx0 = __fmaf_rn(lx, r.ix, -r.oix), tx1 = __fmaf_rn(hx, r.ix, -r.oix);
-  const float ty0 = __fmaf_rn(ly, r.iy, -r.oiy), ty1 = __fmaf_rn(hy, r.iy, -r.oiy);
-  const float tz0 = __fmaf_rn(lz, r.iz, -r.oiz), tz1 = __fmaf_rn(hz, r.iz, -r.oiz);
-  const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.f));
-  float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+// Each axis' near and far plane is chosen by the sign of the inverse
+// direction (near = lo where it is positive). For a finite inverse direction
+// the entry / exit distances equal the min / max of the two planes'; for an
+// infinite one (a zero direction component) they are NaN or infinite, and the
+// NaN-skipping fminf / fmaxf then leave the axis unconstrained unless the
+// parallel ray lies outside the slab.
+__device__ __forceinline__ bool box_hit_nf(const Ray& r, float nx, float fx, float ny, float fy,
+                                           float nz, float fz, float& tentry) {
+  const float tn = fmaxf(fmaxf(__fmaf_rn(nx, r.ix, -r.oix), __fmaf_rn(ny, r.iy, -r.oiy)),
+                         fmaxf(__fmaf_rn(nz, r.iz, -r.oiz), 0.f));
+  float tf = fminf(fminf(__fmaf_rn(fx, r.ix, -r.oix), __fmaf_rn(fy, r.iy, -r.oiy)),
+                   __fmaf_rn(fz, r.iz, -r.oiz));
   tf = fminf(__fmul_rn(tf, 1.00000072f), r.tfar);
   tentry = tn;
   return tn <= tf;
+}
+
+// The same test on a box given as (lo, hi) per axis.
+__device__ __forceinline__ bool box_hit(const Ray& r, float lx, float hx, float ly, float hy,
+                                        float lz, float hz, float& tentry) {
+  return box_hit_nf(r, r.nx ? hx : lx, r.nx ? lx : hx, r.ny ? hy : ly, r.ny ? ly : hy,
+                    r.nz ? hz : lz, r.nz ? lz : hz, tentry);
 }
 
 template <bool kCount>
@@ -378,17 +394,19 @@ __device__ __forceinline__ bool visit_node(const Node* __restrict__ nodes, const
 // on stack overflow.
 __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, const Ray& r,
                                             int& ref, int* stack, int& sp) {
-  const Node4* nd = nodes4 + ref;
-  const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix);
-  const float4 ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
-  const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
-  const int4 ch = __ldg(&nd->child);
+  // Planes in node order lo.x, hi.x, lo.y, hi.y, lo.z, hi.z: the near plane
+  // of an axis is lo + n (n = 1 for a negative inverse direction).
+  const float4* pl = reinterpret_cast<const float4*>(nodes4 + ref);
+  const float4 nx = __ldg(pl + r.nx), fx = __ldg(pl + 1 - r.nx);
+  const float4 ny = __ldg(pl + 2 + r.ny), fy = __ldg(pl + 3 - r.ny);
+  const float4 nz = __ldg(pl + 4 + r.nz), fz = __ldg(pl + 5 - r.nz);
+  const int4 ch = __ldg(&nodes4[ref].child);
   float t0, t1, t2, t3;
   int r0 = ch.x, r1 = ch.y, r2 = ch.z, r3 = ch.w;
-  if (!(r0 != kEmptyRef && box_hit(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, t0))) t0 = INFINITY;
-  if (!(r1 != kEmptyRef && box_hit(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, t1))) t1 = INFINITY;
-  if (!(r2 != kEmptyRef && box_hit(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, t2))) t2 = INFINITY;
-  if (!(r3 != kEmptyRef && box_hit(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, t3))) t3 = INFINITY;
+  if (!(r0 != kEmptyRef && box_hit_nf(r, nx.x, fx.x, ny.x, fy.x, nz.x, fz.x, t0))) t0 = INFINITY;
+  if (!(r1 != kEmptyRef && box_hit_nf(r, nx.y, fx.y, ny.y, fy.y, nz.y, fz.y, t1))) t1 = INFINITY;
+  if (!(r2 != kEmptyRef && box_hit_nf(r, nx.z, fx.z, ny.z, fy.z, nz.z, fz.z, t2))) t2 = INFINITY;
+  if (!(r3 != kEmptyRef && box_hit_nf(r, nx.w, fx.w, ny.w, fy.w, nz.w, fz.w, t3))) t3 = INFINITY;
   // Sorting network on (t, ref): (0,1) (2,3) (0,2) (1,3) (1,2).
   auto cx = [](float& ta, int& ra, float& tb, int& rb) {
     const bool sw = tb < ta;
@@ -462,6 +480,12 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   const float4* tri_lo = nullptr;
   Ray r;
   unsigned long long rays = 0, nvis = 0, ntest = 0;
+#ifdef HZ_DIAG
+  // Per-warp loop statistics: iterations, node passes, node lanes, triangle
+  // passes, triangle lanes, advance passes, advancing lanes, live lanes,
+  // tracing lanes (summed over iterations).
+  unsigned long long dg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#endif
 
   // A leaf target becomes the postponed leaf when the lane holds none; a ray
   // with neither a target nor a postponed leaf has missed.
@@ -481,6 +505,15 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     const unsigned live = __ballot_sync(kFull, alive);
     if (live == 0u) break;
     const unsigned waiting = __ballot_sync(kFull, alive && need);
+#ifdef HZ_DIAG
+    dg[0]++;
+    dg[7] += __popc(live);
+    dg[8] += __popc(live & ~waiting);
+    if (waiting != 0u && (__popc(waiting) >= advance_min || waiting == live)) {
+      dg[5]++;
+      dg[6] += __popc(waiting);
+    }
+#endif
     if (waiting != 0u && (__popc(waiting) >= advance_min || waiting == live) && alive && need) {
       int dom = si[0][t], cell = si[1][t], a = si[2][t], phase = si[3][t], up = si[4][t];
       int m = si[5][t];
@@ -642,6 +675,15 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     }
 
     // Node pass.
+#ifdef HZ_DIAG
+    {
+      const unsigned nl = __ballot_sync(kFull, alive && !need && ref >= 0);
+      if (nl) {
+        dg[1]++;
+        dg[2] += __popc(nl);
+      }
+    }
+#endif
     if (alive && !need && ref >= 0) {
       if (kCount) nvis++;
       if (!(kWide ? visit_node4(nodes4, r, ref, stack, sp)
@@ -658,6 +700,12 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     const unsigned pend = __ballot_sync(kFull, has_leaf);
     if (pend != 0u) {
       const unsigned nodes_left = __ballot_sync(kFull, alive && !need && ref >= 0);
+#ifdef HZ_DIAG
+      if (__popc(pend) >= leaf_min || nodes_left == 0u) {
+        dg[3]++;
+        dg[4] += __popc(pend);
+      }
+#endif
       if ((__popc(pend) >= leaf_min || nodes_left == 0u) && has_leaf) {
         if (kCount) ntest++;
         const bool hit = test_tri<kPrecise>(tris, tri_lo, r, pst);
@@ -683,6 +731,9 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
       atomicAdd(&counters[1], nvis);
       atomicAdd(&counters[2], ntest);
     }
+#ifdef HZ_DIAG
+    for (int q = 0; q < 9; q++) atomicAdd(&counters[3 + q], dg[q]);
+#endif
   }
 }
 

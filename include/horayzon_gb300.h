@@ -72,6 +72,7 @@ typedef struct hz_options {
     int32_t leaf_min;        /* persistent kernel: lanes of a warp that must hold a
                                 postponed leaf before a triangle pass (1..32; 0 =
                                 library default) */
+    int32_t leaf_size;       /* most triangles per BVH leaf (1..8; 0 = 2) */
 } hz_options;
 
 enum {
@@ -130,6 +131,24 @@ void horizon_svf_comp(double* clon, double* clat, double* hsurf,
                       int grid_type, double dist_search,
                       double ray_org_elev, int refine_factor,
                       int svf_type);
+
+/*
+ * The reference's dormant Fortran variant (mo_lradtopo_horayzon.cpp:561-574,
+ * 778-784): the same computation, with the progress lines that
+ * horizon_svf_comp prints (with HZ_VERBOSE=1) captured into the caller's
+ * buffer instead of stdout. On entry *buffer_len is the buffer's capacity; on
+ * return it is the number of bytes written (the first *buffer_len bytes of
+ * the text, no terminating NUL). Errors append "horizon_svf_comp: <message>"
+ * to the text and fill horizon and skyview with NaN.
+ */
+void horizon_svf_comp_buffer(double* clon, double* clat, double* hsurf,
+                             double* vlon, double* vlat,
+                             int* cells_of_vertex,
+                             double* horizon, double* skyview,
+                             int num_cell, int num_vertex, int num_hori,
+                             int grid_type, double dist_search,
+                             double ray_org_elev, int refine_factor,
+                             int svf_type, char* buffer, int* buffer_len);
 
 /*
  * Same computation with a status, options and statistics. Host buffers; the

@@ -235,3 +235,34 @@ def test_gpu_batch_equals_single_calls():
         np.testing.assert_array_equal(s, s1)
         rays += st1["num_rays"]
     assert st["num_rays"] == rays
+
+
+@pytest.mark.parametrize("kernel,leaf_size", [(0, 1), (0, 2), (0, 8), (2, 3), (1, 8)])
+def test_gpu_leaf_size_keeps_results(small_domain, kernel, leaf_size):
+    """Triangles per BVH leaf change the tree, not the rays or hit decisions."""
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    h0, s0, st0 = horizon_svf_comp_py(*small_domain.inputs(), *args, return_stats=True)
+    h1, s1, st1 = horizon_svf_comp_py(*small_domain.inputs(), *args, kernel=kernel,
+                                      leaf_size=leaf_size, return_stats=True)
+    np.testing.assert_array_equal(h0, h1)
+    np.testing.assert_allclose(s0, s1, rtol=0, atol=1e-12)
+    assert st0["num_rays"] == st1["num_rays"]
+
+
+def test_gpu_autotune_picks_a_grid_setting(small_domain, tmp_path, monkeypatch):
+    torch = pytest.importorskip("torch")
+    from horayzon_extpar_gb300 import autotune, horizon_svf_comp_device
+    monkeypatch.setenv("HZ_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    t = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in small_domain.inputs()]
+    grid = {"leaf_size": (4, 2), "advance_min": (16, 8), "leaf_min": (12, 6),
+            "kernel": (0, 2)}
+    res = autotune.tune(t, args, sample_cells=500, reps=1, rounds=1, grid=grid)
+    assert not res["cached"] and res["trials"] >= 5
+    for k, v in grid.items():
+        assert res[k] in v
+    again = autotune.tune(t, args, grid=grid)
+    assert again["cached"] and autotune.knobs(again) == autotune.knobs(res)
+    h0, s0, _ = horizon_svf_comp_device(*t, *args)
+    h1, s1, _ = horizon_svf_comp_device(*t, *args, **autotune.knobs(res))
+    assert torch.equal(h0, h1)
