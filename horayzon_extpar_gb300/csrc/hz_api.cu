@@ -410,6 +410,9 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     const unsigned long long tot = pr[d].nvert > 0 ? pin_tot[d] : 0ull;
     out->n_tri[d] = (int)(tot & 0xFFFFFFFFull);
     nadd[d] = (int)(tot >> 32);
+    // Leaf references and postponed leaves keep a triangle index in 27 bits.
+    if (out->n_tri[d] >= (1 << 27))
+      return fail(HZ_ERR_VALUE, "mesh of %d triangles exceeds 2^27 per domain", out->n_tri[d]);
     out->n_mv[d] = pr[d].ncell + nadd[d];
   }
   for (int d = 0; d < n; d++) {

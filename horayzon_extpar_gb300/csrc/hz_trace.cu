@@ -472,7 +472,9 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
 
   bool alive = true, need = true, last_hit = false;
   int ref = kEmptyRef, sp = 0;
-  int pst = 0, pcnt = 0;  // postponed leaf: next triangle, triangles left
+  // Postponed leaves (up to two), each as next triangle << 4 | triangles
+  // left (0 = free); slot 1 is used only while slot 0 is occupied.
+  int pl0 = 0, pl1 = 0;
   int stack[kWide ? kStackDepth4 : kStackDepth];
   const Node* nodes = nullptr;
   const Node4* nodes4 = nullptr;
@@ -487,15 +489,19 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   unsigned long long dg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 #endif
 
-  // A leaf target becomes the postponed leaf when the lane holds none; a ray
-  // with neither a target nor a postponed leaf has missed.
+  // A leaf target is postponed while a slot is free and the lane continues
+  // from its stack; a ray with neither a target nor a postponed leaf has
+  // missed.
   auto settle = [&]() {
-    if (ref < 0 && ref != kEmptyRef && pcnt == 0) {
-      pst = leaf_start(ref);
-      pcnt = leaf_count(ref);
+    if (ref < 0 && ref != kEmptyRef && pl0 == 0) {
+      pl0 = (leaf_start(ref) << 4) | leaf_count(ref);
       ref = sp > 0 ? stack[--sp] : kEmptyRef;
     }
-    if (ref == kEmptyRef && pcnt == 0) {
+    if (ref < 0 && ref != kEmptyRef && pl1 == 0) {
+      pl1 = (leaf_start(ref) << 4) | leaf_count(ref);
+      ref = sp > 0 ? stack[--sp] : kEmptyRef;
+    }
+    if (ref == kEmptyRef && pl0 == 0) {
       need = true;
       last_hit = false;
     }
@@ -595,8 +601,10 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
           if (h < 0.0) h = 0.0;
           double sector = sv[13][t] + h;
           if ((a + 1) % D.refine == 0) {
+            // x / 1.0 == x exactly, so the division is skipped for refine 1.
+            const double deg = (sector / kPi) * 180.0;
             D.horizon[(long long)(a / D.refine) * D.ncell + cell] =
-                ((sector / kPi) * 180.0) / (double)D.refine;
+                D.refine == 1 ? deg : deg / (double)D.refine;
             sector = 0.0;
           }
           double s = 0.0;
@@ -667,7 +675,8 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
           r = make_ray(so[0][t], so[1][t], so[2][t], dx, dy, dz, D.tfar);
         ref = D.root;
         sp = 0;
-        pcnt = 0;
+        pl0 = 0;
+        pl1 = 0;
         need = false;
         rays++;
         settle();
@@ -696,7 +705,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
       }
     }
     // Triangle pass.
-    const bool has_leaf = alive && !need && pcnt > 0;
+    const bool has_leaf = alive && !need && pl0 != 0;
     const unsigned pend = __ballot_sync(kFull, has_leaf);
     if (pend != 0u) {
       const unsigned nodes_left = __ballot_sync(kFull, alive && !need && ref >= 0);
@@ -708,13 +717,14 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
 #endif
       if ((__popc(pend) >= leaf_min || nodes_left == 0u) && has_leaf) {
         if (kCount) ntest++;
-        const bool hit = test_tri<kPrecise>(tris, tri_lo, r, pst);
-        pst++;
-        pcnt--;
+        const bool hit = test_tri<kPrecise>(tris, tri_lo, r, pl0 >> 4);
+        pl0 += (1 << 4) - 1;  // next triangle, one fewer left
         if (hit) {
           need = true;
           last_hit = true;
-        } else if (pcnt == 0) {
+        } else if ((pl0 & 15) == 0) {
+          pl0 = pl1;
+          pl1 = 0;
           settle();
         }
       }

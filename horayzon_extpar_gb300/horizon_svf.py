@@ -253,7 +253,7 @@ def mesh_enu32(clon, clat, hsurf, vlon, vlat, cells_of_vertex, grid_type, device
 
 def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_deg=-85.0,
                            advance_min=0, return_stats=False, precision=0, mlp_params=None,
-                           mlp_every_azimuth=False):
+                           mlp_every_azimuth=False, kernel=0, leaf_min=0, leaf_size=0):
     """Many independent domains in one call (one persistent search launch).
 
     ``domains``: sequence of ``(inputs, args)`` with ``inputs`` the six arrays
@@ -279,8 +279,9 @@ def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_d
             arrs[0].size, arrs[3].size, int(num_hori), int(grid_type), float(dist_search),
             float(ray_org_elev), int(refine), int(svf), 0.0))
     arr = (_lib.Domain * len(structs))(*structs)
-    opt = _options(device, count_work, elev_floor_deg, False, None, 0, advance_min, precision,
-                   mlp_params, mlp_every_azimuth=mlp_every_azimuth)
+    opt = _options(device, count_work, elev_floor_deg, False, None, kernel, advance_min,
+                   precision, mlp_params, mlp_every_azimuth=mlp_every_azimuth,
+                   leaf_min=leaf_min, leaf_size=leaf_size)
     st = _lib.Stats()
     rc = _lib.load().hz_horizon_svf_batch(arr, len(structs), 0, None, C.byref(opt),
                                           C.byref(st))
