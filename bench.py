@@ -217,12 +217,22 @@ def precision_report(dom, d_in, h_ref, s_ref, stream, sample=20000):
                                                     replace=False))
     h64, s64, _ = oracle.horizon_svf(*dom.inputs(), *ARGS, precision=1, cells=cells)
 
+    # Cells whose 40 km search reaches the domain edge (functions.py:58-97,
+    # verification.py:302-304) are reported separately.
+    from horayzon_extpar_gb300.border import distance_to_border
+    dist = distance_to_border(dom.clon, dom.clat, dom.vlon, dom.vlat, dom.cells_of_vertex)
+    inner = dist[cells] >= ARGS[2] * 1e-3
+
     def stats(h, s):
         dh = np.abs(h[:, cells] - h64[:, cells])
         ds = np.abs(s[cells] - s64[cells])
         return {"frac_evals_differing": float(np.mean(dh > 1e-9)),
                 "max_abs_deg": float(dh.max()), "mean_abs_deg": float(dh.mean()),
-                "max_abs_svf": float(ds.max()), "mean_abs_svf": float(ds.mean())}
+                "max_abs_svf": float(ds.max()), "mean_abs_svf": float(ds.mean()),
+                "border_masked": {"cells": int(inner.sum()),
+                                  "frac_evals_differing": float(np.mean(dh[:, inner] > 1e-9)),
+                                  "max_abs_deg": float(dh[:, inner].max()),
+                                  "max_abs_svf": float(ds[inner].max())}}
 
     d = np.abs(h_loc - h_ref)
     return {"oracle": "FP64 vertices, rays and triangle test (oracle/hz_oracle.c)",

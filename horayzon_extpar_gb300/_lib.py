@@ -24,7 +24,8 @@ EXPORTED_SYMBOLS = ("hz_default_options", "horizon_svf_comp", "horizon_svf_comp_
                     "hz_horizon_svf_device", "hz_build_mesh", "hz_mesh_enu32",
                     "hz_last_error", "hz_version", "hz_release_workspace",
                     "hz_horizon_svf_device_static", "hz_horizon_svf_batch",
-                    "hz_mlp_num_params", "hz_mlp_train_step", "hz_mlp_forward")
+                    "hz_mlp_num_params", "hz_mlp_train_step", "hz_mlp_forward",
+                    "hz_distance_to_border")
 
 
 class Domain(C.Structure):
@@ -121,6 +122,9 @@ def load(build_if_missing: bool = True):
         L.hz_horizon_svf_batch.restype = C.c_int
         L.hz_horizon_svf_batch.argtypes = [C.POINTER(Domain), C.c_int, C.c_int, C.c_void_p,
                                            C.POINTER(Options), C.POINTER(Stats)]
+        L.hz_distance_to_border.restype = C.c_int
+        L.hz_distance_to_border.argtypes = [C.c_void_p] * 5 + [C.c_int, C.c_int, C.c_void_p,
+                                                               C.c_int, C.c_void_p]
         L.hz_mlp_num_params.restype = C.c_int
         L.hz_mlp_num_params.argtypes = []
         L.hz_mlp_train_step.restype = C.c_int

@@ -472,9 +472,8 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
 
   bool alive = true, need = true, last_hit = false;
   int ref = kEmptyRef, sp = 0;
-  // Postponed leaves (up to two), each as next triangle << 4 | triangles
-  // left (0 = free); slot 1 is used only while slot 0 is occupied.
-  int pl0 = 0, pl1 = 0;
+  // Postponed leaf as next triangle << 4 | triangles left (0 = none).
+  int pl0 = 0;
   int stack[kWide ? kStackDepth4 : kStackDepth];
   const Node* nodes = nullptr;
   const Node4* nodes4 = nullptr;
@@ -489,16 +488,12 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   unsigned long long dg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 #endif
 
-  // A leaf target is postponed while a slot is free and the lane continues
-  // from its stack; a ray with neither a target nor a postponed leaf has
-  // missed.
+  // A leaf target is postponed when the lane holds none and the lane
+  // continues from its stack; a ray with neither a target nor a postponed
+  // leaf has missed.
   auto settle = [&]() {
     if (ref < 0 && ref != kEmptyRef && pl0 == 0) {
       pl0 = (leaf_start(ref) << 4) | leaf_count(ref);
-      ref = sp > 0 ? stack[--sp] : kEmptyRef;
-    }
-    if (ref < 0 && ref != kEmptyRef && pl1 == 0) {
-      pl1 = (leaf_start(ref) << 4) | leaf_count(ref);
       ref = sp > 0 ? stack[--sp] : kEmptyRef;
     }
     if (ref == kEmptyRef && pl0 == 0) {
@@ -676,7 +671,6 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
         ref = D.root;
         sp = 0;
         pl0 = 0;
-        pl1 = 0;
         need = false;
         rays++;
         settle();
@@ -723,8 +717,6 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
           need = true;
           last_hit = true;
         } else if ((pl0 & 15) == 0) {
-          pl0 = pl1;
-          pl1 = 0;
           settle();
         }
       }

@@ -112,6 +112,21 @@ typedef struct hz_stats {
     int64_t kernel_launches; /* CUDA kernels this call launched */
 } hz_stats;
 
+/*
+ * Distance of every cell circumcentre to the mesh border, replacing
+ * functions.distance_to_border (functions.py:58-97): the chord distance [km]
+ * on a sphere of radius 6371.0087714 km from each cell to the nearest ICON
+ * vertex that has a missing neighbour cell (a -2 in cells_of_vertex); +inf
+ * when no vertex has one. Arrays as in horizon_svf_comp; dist[num_cell].
+ * on_device != 0: all pointers are device pointers and the work runs on
+ * `stream`; otherwise host pointers.
+ */
+int hz_distance_to_border(const double* clon, const double* clat,
+                          const double* vlon, const double* vlat,
+                          const int32_t* cells_of_vertex, int num_cell,
+                          int num_vertex, double* dist, int on_device,
+                          void* stream);
+
 /* Fills *opt with the defaults (device -1, elev_floor_deg -85, counters off). */
 void hz_default_options(hz_options* opt);
 

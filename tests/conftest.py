@@ -17,8 +17,9 @@ def pytest_configure(config):
 
 
 def golden_cases():
+    """Horizon/SVF fixtures (make_golden.py); border_golden.npz is separate."""
     return sorted(os.path.splitext(os.path.basename(p))[0]
-                  for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
+                  for p in glob.glob(os.path.join(GOLDEN_DIR, "g*.npz")))
 
 
 def load_golden(name):
