@@ -9,6 +9,8 @@ decision is the watertight test's):
   together;
 * ``leaf_min``: lanes of a warp that must hold a postponed leaf before a
   triangle pass runs;
+* ``queue_chunk``: consecutive cells (Morton order) a warp takes from the
+  work queue at a time;
 * ``kernel``: the 4-wide or the binary BVH.
 
 :func:`tune` times the device entry point on a contiguous sample of the
@@ -32,9 +34,10 @@ GRID = {
     "leaf_size": (2, 1, 3, 4, 6),
     "advance_min": (16, 8, 12, 20, 24),
     "leaf_min": (12, 6, 8, 16, 20),
+    "queue_chunk": (32, 1, 64, 128),
     "kernel": (_lib.HZ_KERNEL_PERSISTENT, _lib.HZ_KERNEL_PERSISTENT_BVH2),
 }
-DEFAULTS = {"leaf_size": 2, "advance_min": 16, "leaf_min": 12,
+DEFAULTS = {"leaf_size": 2, "advance_min": 16, "leaf_min": 12, "queue_chunk": 32,
             "kernel": _lib.HZ_KERNEL_PERSISTENT}
 _lock = threading.Lock()
 

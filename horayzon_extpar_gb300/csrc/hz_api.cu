@@ -604,7 +604,8 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       desc[d] = D;
       total += P.cell_count;
     }
-    if (total > INT32_MAX) return fail(HZ_ERR_VALUE, "more than 2^31 cells in one call");
+    if (total > INT32_MAX - (1ll << 26))
+      return fail(HZ_ERR_VALUE, "more than 2^31 - 2^26 cells in one call");
     HZ_CUDA(cudaMemcpyAsync(bb.doms, desc, sizeof(DomainDesc) * (size_t)n,
                             cudaMemcpyHostToDevice, s));
     const int adv =
@@ -614,8 +615,9 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     k_stamp<<<1, 1, 0, s>>>(bb.t0);
     note_launches(1);
     HZ_CUDA(cudaGetLastError());
-    HZ_CUDA(trace_flat(bb.doms, n, bb.order, (int)total, bb.work, bb.counters, bb.err, adv,
-                       leaf, variant, opt.count_work != 0, b[0].tri_lo != nullptr, s));
+    const TraceKnobs knobs{adv, leaf, opt.queue_chunk, variant};
+    HZ_CUDA(trace_flat(bb.doms, n, bb.order, (int)total, bb.work, bb.counters, bb.err, knobs,
+                       opt.count_work != 0, b[0].tri_lo != nullptr, s));
   }
   HZ_CUDA(cudaEventRecord(E.ev[3], s));
 

@@ -149,9 +149,10 @@ struct DomainDesc {
 // `total` work ids from `order`; a work id is cell_offset + cell of its
 // domain, and `doms` is sorted by cell_offset.
 // precise: every domain carries tri_lo and rays use hi + lo vertices/origin.
-// variant: the BVH the search traverses (kTrace*); advance_min / leaf_min:
-// lanes of a warp that must be waiting before the search state advances /
-// holding a postponed leaf before a triangle pass runs.
+// k.variant: the BVH the search traverses (kTrace*); k.advance_min /
+// k.leaf_min: lanes of a warp that must be waiting before the search state
+// advances / holding a postponed leaf before a triangle pass runs; k.chunk:
+// consecutive work ids a warp claims at a time.
 enum : int {
   kTraceWide = 0,   // 4-wide BVH (DomainDesc::nodes4)
   kTraceBinary = 1  // binary BVH (DomainDesc::nodes)
@@ -161,10 +162,16 @@ enum : int {
 constexpr int kCounterWords = 16;
 constexpr int kDefaultAdvanceMin = 16;
 constexpr int kDefaultLeafMin = 12;
+constexpr int kDefaultChunk = 32;
+struct TraceKnobs {
+  int advance_min;  // 1..32
+  int leaf_min;     // 1..32
+  int chunk;        // work ids a warp claims per atomic (< 1: kDefaultChunk)
+  int variant;      // kTraceWide / kTraceBinary
+};
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
-                       int* work, unsigned long long* counters, int* err, int advance_min,
-                       int leaf_min, int variant, bool count_work, bool precise,
-                       cudaStream_t s);
+                       int* work, unsigned long long* counters, int* err, const TraceKnobs& k,
+                       bool count_work, bool precise, cudaStream_t s);
 
 // ---- hz_learn.cu ------------------------------------------------------------
 constexpr int kMlpIn = 32;

@@ -293,9 +293,9 @@ extern "C" int hz_horizon_svf_device_static(
                             b.work, s), "cell order");
   HZ_STATIC_CUDA(trace_tables(b.azim_cs, b.elev_cs, b.sin_lattice, L, azim_shift, D.hori_acc,
                               s), "lattice tables");
-  HZ_STATIC_CUDA(trace_flat(b.dom, 1, b.order, num_cell, b.work, b.counters, b.err,
-                            kDefaultAdvanceMin, kDefaultLeafMin, kTraceBinary, false, false,
-                            s), "horizon search");
+  const TraceKnobs knobs{kDefaultAdvanceMin, kDefaultLeafMin, kDefaultChunk, kTraceBinary};
+  HZ_STATIC_CUDA(trace_flat(b.dom, 1, b.order, num_cell, b.work, b.counters, b.err, knobs,
+                            false, false, s), "horizon search");
   HZ_STATIC_CUDA(cudaMemcpyAsync(&err, b.err, sizeof(int), cudaMemcpyDeviceToHost, s),
                  "reading error word");
   HZ_STATIC_CUDA(cudaStreamSynchronize(s), "horizon search");

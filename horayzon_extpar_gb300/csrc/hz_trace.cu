@@ -359,6 +359,10 @@ constexpr int kFlatBlock = 128;
 #define HZ_WARP_MIN_BLOCKS 6  // resident blocks per SM the register budget targets
 #endif
 
+#ifndef HZ_NODE4_ORDER
+#define HZ_NODE4_ORDER 0  // 0: hit children sorted by entry distance; 1: nearest first only
+#endif
+
 enum : int { kPhaseStart = 0, kPhaseFirst = 1, kPhaseUp = 2, kPhaseDown = 3 };
 
 // Visits internal node `ref`: descends into the nearer hit child (pushing the
@@ -407,7 +411,6 @@ __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, co
   if (!(r1 != kEmptyRef && box_hit_nf(r, nx.y, fx.y, ny.y, fy.y, nz.y, fz.y, t1))) t1 = INFINITY;
   if (!(r2 != kEmptyRef && box_hit_nf(r, nx.z, fx.z, ny.z, fy.z, nz.z, fz.z, t2))) t2 = INFINITY;
   if (!(r3 != kEmptyRef && box_hit_nf(r, nx.w, fx.w, ny.w, fy.w, nz.w, fz.w, t3))) t3 = INFINITY;
-  // Sorting network on (t, ref): (0,1) (2,3) (0,2) (1,3) (1,2).
   auto cx = [](float& ta, int& ra, float& tb, int& rb) {
     const bool sw = tb < ta;
     const float t = sw ? tb : ta;
@@ -417,11 +420,19 @@ __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, co
     ta = t;
     ra = q;
   };
+#if HZ_NODE4_ORDER == 1
+  // Nearest hit child first; the others keep their slot order.
+  cx(t0, r0, t1, r1);
+  cx(t0, r0, t2, r2);
+  cx(t0, r0, t3, r3);
+#else
+  // Sorting network on (t, ref): (0,1) (2,3) (0,2) (1,3) (1,2).
   cx(t0, r0, t1, r1);
   cx(t2, r2, t3, r3);
   cx(t0, r0, t2, r2);
   cx(t1, r1, t3, r3);
   cx(t1, r1, t2, r2);
+#endif
   if (t0 == INFINITY) {
     ref = sp > 0 ? stack[--sp] : kEmptyRef;
     return true;
@@ -455,7 +466,7 @@ template <bool kCount, bool kPrecise, bool kWide>
 __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     k_trace_warp(const DomainDesc* __restrict__ doms, int ndom, const int* __restrict__ order,
                  int total, int* __restrict__ work, unsigned long long* __restrict__ counters,
-                 int* __restrict__ err, int advance_min, int leaf_min) {
+                 int* __restrict__ err, int advance_min, int leaf_min, int chunk) {
   // Per-lane search state. FP64: 0-2 sphere normal U, 3-5 north N, 6-8 east
   // E, 9-11 horizontal direction of the current azimuth, 12 elevation
   // accumulator, 13 sector sum, 14 SVF sum. Integers: domain, cell, azimuth,
@@ -464,8 +475,14 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   __shared__ double sv[15][kFlatBlock];
   __shared__ int si[6][kFlatBlock];
   __shared__ float so[6][kFlatBlock];
+  __shared__ int wq[2][kFlatBlock / 32];  // per warp: next and end of its chunk of work ids
   constexpr unsigned kFull = 0xffffffffu;
   const int t = threadIdx.x;
+  if ((t & 31) == 0) {
+    wq[0][t >> 5] = 0;
+    wq[1][t >> 5] = 0;
+  }
+  __syncwarp();
 #pragma unroll
   for (int q = 0; q < 6; q++) si[q][t] = 0;
   si[3][t] = kPhaseStart;
@@ -515,13 +532,41 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
       dg[6] += __popc(waiting);
     }
 #endif
-    if (waiting != 0u && (__popc(waiting) >= advance_min || waiting == live) && alive && need) {
+    const bool advance = waiting != 0u && (__popc(waiting) >= advance_min || waiting == live);
+    // Cells for the lanes that start one: consecutive work ids (Morton order)
+    // from the warp's chunk, refilled with one atomic of `chunk` ids.
+    int k_new = 0;
+    if (advance) {
+      const unsigned starting = __ballot_sync(kFull, alive && need && si[3][t] == kPhaseStart);
+      if (starting != 0u) {
+        const int lane = t & 31, w = t >> 5;
+        const int nreq = __popc(starting);
+        int first = 0, take = 0, nb = 0;
+        if (lane == 0) {
+          take = min(wq[1][w] - wq[0][w], nreq);
+          first = wq[0][w];
+          wq[0][w] += take;
+          if (take < nreq) {
+            const int grab = max(chunk, nreq - take);
+            nb = atomicAdd(work, grab);
+            wq[0][w] = nb + (nreq - take);
+            wq[1][w] = nb + grab;
+          }
+        }
+        first = __shfl_sync(kFull, first, 0);
+        take = __shfl_sync(kFull, take, 0);
+        nb = __shfl_sync(kFull, nb, 0);
+        const int rank = __popc(starting & ((1u << lane) - 1u));
+        k_new = rank < take ? first + rank : nb + (rank - take);
+      }
+    }
+    if (advance && alive && need) {
       int dom = si[0][t], cell = si[1][t], a = si[2][t], phase = si[3][t], up = si[4][t];
       int m = si[5][t];
       bool emit = false;
       while (!emit) {
         if (phase == kPhaseStart) {
-          const int k = atomicAdd(work, 1);
+          const int k = k_new;
           if (k >= total) {
             alive = false;
             break;
@@ -620,8 +665,9 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
                 D.done[1] = now;
               }
             }
+            // The next cell comes from the warp's chunk in the next pass.
             phase = kPhaseStart;
-            continue;
+            break;
           }
           sv[13][t] = sector;
           sv[14][t] = svf;
@@ -641,7 +687,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
         emit = true;
       }
       si[3][t] = phase;
-      if (alive) {
+      if (alive && emit) {
         si[0][t] = dom;
         si[1][t] = cell;
         si[2][t] = a;
@@ -717,6 +763,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
           need = true;
           last_hit = true;
         } else if ((pl0 & 15) == 0) {
+          pl0 = 0;  // leaf done: the slot is free again
           settle();
         }
       }
@@ -869,28 +916,31 @@ cudaError_t launch_persistent(void (*kernel)(P...), int total, cudaStream_t s, A
 template <bool kCount, bool kPrecise>
 cudaError_t launch_variant(const DomainDesc* doms, int ndom, const int32_t* order, int total,
                            int* work, unsigned long long* counters, int* err, int advance_min,
-                           int leaf_min, int variant, cudaStream_t s) {
+                           int leaf_min, int chunk, int variant, cudaStream_t s) {
   if (variant == kTraceWide)
     return launch_persistent(k_trace_warp<kCount, kPrecise, true>, total, s, doms, ndom, order,
-                             total, work, counters, err, advance_min, leaf_min);
+                             total, work, counters, err, advance_min, leaf_min, chunk);
   return launch_persistent(k_trace_warp<kCount, kPrecise, false>, total, s, doms, ndom, order,
-                           total, work, counters, err, advance_min, leaf_min);
+                           total, work, counters, err, advance_min, leaf_min, chunk);
 }
 
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
-                       int* work, unsigned long long* counters, int* err, int advance_min,
-                       int leaf_min, int variant, bool count_work, bool precise,
-                       cudaStream_t s) {
+                       int* work, unsigned long long* counters, int* err, const TraceKnobs& k,
+                       bool count_work, bool precise, cudaStream_t s) {
   if (total <= 0 || ndom <= 0) return cudaSuccess;
+  const int c = k.chunk >= 1 ? k.chunk : kDefaultChunk;
   if (precise)
     return count_work ? launch_variant<true, true>(doms, ndom, order, total, work, counters,
-                                                   err, advance_min, leaf_min, variant, s)
+                                                   err, k.advance_min, k.leaf_min, c, k.variant,
+                                                   s)
                       : launch_variant<false, true>(doms, ndom, order, total, work, counters,
-                                                    err, advance_min, leaf_min, variant, s);
+                                                    err, k.advance_min, k.leaf_min, c, k.variant,
+                                                    s);
   return count_work ? launch_variant<true, false>(doms, ndom, order, total, work, counters, err,
-                                                  advance_min, leaf_min, variant, s)
+                                                  k.advance_min, k.leaf_min, c, k.variant, s)
                     : launch_variant<false, false>(doms, ndom, order, total, work, counters,
-                                                   err, advance_min, leaf_min, variant, s);
+                                                   err, k.advance_min, k.leaf_min, c, k.variant,
+                                                   s);
 }
 
 cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s) {

@@ -73,6 +73,8 @@ typedef struct hz_options {
                                 postponed leaf before a triangle pass (1..32; 0 =
                                 library default) */
     int32_t leaf_size;       /* most triangles per BVH leaf (1..8; 0 = 2) */
+    int32_t queue_chunk;     /* persistent kernel: consecutive cells (Morton order) a
+                                warp takes from the work queue at a time (0 = 32) */
 } hz_options;
 
 enum {

@@ -256,7 +256,7 @@ def test_gpu_autotune_picks_a_grid_setting(small_domain, tmp_path, monkeypatch):
     args = (24, 1, 40000.0, 0.2, 1, 2)
     t = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in small_domain.inputs()]
     grid = {"leaf_size": (4, 2), "advance_min": (16, 8), "leaf_min": (12, 6),
-            "kernel": (0, 2)}
+            "queue_chunk": (32, 1), "kernel": (0, 2)}
     res = autotune.tune(t, args, sample_cells=500, reps=1, rounds=1, grid=grid)
     assert not res["cached"] and res["trials"] >= 5
     for k, v in grid.items():
@@ -266,3 +266,16 @@ def test_gpu_autotune_picks_a_grid_setting(small_domain, tmp_path, monkeypatch):
     h0, s0, _ = horizon_svf_comp_device(*t, *args)
     h1, s1, _ = horizon_svf_comp_device(*t, *args, **autotune.knobs(res))
     assert torch.equal(h0, h1)
+
+
+@pytest.mark.parametrize("queue_chunk", [1, 7, 64])
+def test_gpu_queue_chunk_keeps_results(small_domain, queue_chunk):
+    """How many cells a warp takes from the work queue at a time changes the
+    schedule only."""
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    h0, s0, st0 = horizon_svf_comp_py(*small_domain.inputs(), *args, return_stats=True)
+    h1, s1, st1 = horizon_svf_comp_py(*small_domain.inputs(), *args, queue_chunk=queue_chunk,
+                                      return_stats=True)
+    np.testing.assert_array_equal(h0, h1)
+    np.testing.assert_array_equal(s0, s1)
+    assert st0["num_rays"] == st1["num_rays"]
