@@ -359,6 +359,9 @@ constexpr int kFlatBlock = 128;
 #define HZ_WARP_MIN_BLOCKS 6  // resident blocks per SM the register budget targets
 #endif
 
+#ifndef HZ_NODE_STEPS
+#define HZ_NODE_STEPS 1  // node visits per lane in one node pass
+#endif
 #ifndef HZ_NODE4_ORDER
 #define HZ_NODE4_ORDER 0  // 0: hit children sorted by entry distance; 1: nearest first only
 #endif
@@ -733,15 +736,18 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
       }
     }
 #endif
-    if (alive && !need && ref >= 0) {
-      if (kCount) nvis++;
-      if (!(kWide ? visit_node4(nodes4, r, ref, stack, sp)
-                  : visit_node(nodes, r, ref, stack, sp))) {
-        atomicOr(err, kErrStack);
-        need = true;
-        last_hit = true;
-      } else {
-        settle();
+#pragma unroll
+    for (int step = 0; step < HZ_NODE_STEPS; step++) {
+      if (alive && !need && ref >= 0) {
+        if (kCount) nvis++;
+        if (!(kWide ? visit_node4(nodes4, r, ref, stack, sp)
+                    : visit_node(nodes, r, ref, stack, sp))) {
+          atomicOr(err, kErrStack);
+          need = true;
+          last_hit = true;
+        } else {
+          settle();
+        }
       }
     }
     // Triangle pass.
