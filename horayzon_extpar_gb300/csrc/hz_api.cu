@@ -224,12 +224,14 @@ struct Engine {
   cudaEvent_t ev[8] = {};
   unsigned long long* pinned = nullptr;  // readbacks and descriptor staging
   size_t pinned_words = 0;
+  Staging* staging = nullptr;            // pageable caller buffers (host entries)
 
   int init(int dev) {
     device = dev;
     HZ_CUDA(cudaSetDevice(dev));
     HZ_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     for (auto& e : ev) HZ_CUDA(cudaEventCreate(&e));
+    HZ_CUDA(staging_create(&staging));
     return reserve_pinned(4096);
   }
 
@@ -734,20 +736,21 @@ int cell_range(const hz_options& opt, int ncell, int* begin, int* count) {
 }
 
 // Host <-> device staging of one domain for the host entry points.
-int stage_inputs(const hz_domain& h, const Buffers& b, cudaStream_t s) {
+int stage_inputs(Engine& E, const hz_domain& h, const Buffers& b, cudaStream_t s) {
   const size_t nc = (size_t)h.num_cell, nv = (size_t)h.num_vertex;
-  HZ_CUDA(cudaMemcpyAsync(b.clon, h.clon, nc * 8, cudaMemcpyHostToDevice, s));
-  HZ_CUDA(cudaMemcpyAsync(b.clat, h.clat, nc * 8, cudaMemcpyHostToDevice, s));
-  HZ_CUDA(cudaMemcpyAsync(b.hsurf, h.hsurf, nc * 8, cudaMemcpyHostToDevice, s));
+  Staging* st = E.staging;
+  HZ_CUDA(copy_from_host(st, b.clon, h.clon, nc * 8, s));
+  HZ_CUDA(copy_from_host(st, b.clat, h.clat, nc * 8, s));
+  HZ_CUDA(copy_from_host(st, b.hsurf, h.hsurf, nc * 8, s));
   if (nv) {
-    HZ_CUDA(cudaMemcpyAsync(b.vlon, h.vlon, nv * 8, cudaMemcpyHostToDevice, s));
-    HZ_CUDA(cudaMemcpyAsync(b.vlat, h.vlat, nv * 8, cudaMemcpyHostToDevice, s));
-    HZ_CUDA(cudaMemcpyAsync(b.cov, h.cells_of_vertex, nv * 6 * 4, cudaMemcpyHostToDevice, s));
+    HZ_CUDA(copy_from_host(st, b.vlon, h.vlon, nv * 8, s));
+    HZ_CUDA(copy_from_host(st, b.vlat, h.vlat, nv * 8, s));
+    HZ_CUDA(copy_from_host(st, b.cov, h.cells_of_vertex, nv * 6 * 4, s));
   }
   return HZ_OK;
 }
 
-int unstage_outputs(const hz_domain& h, const Buffers& b, int begin, int count,
+int unstage_outputs(Engine& E, const hz_domain& h, const Buffers& b, int begin, int count,
                     cudaStream_t s) {
   const size_t nc = (size_t)h.num_cell;
   if (begin != 0 || count != h.num_cell) {
@@ -757,9 +760,8 @@ int unstage_outputs(const hz_domain& h, const Buffers& b, int begin, int count,
                               (size_t)h.num_hori, cudaMemcpyDeviceToHost, s));
     HZ_CUDA(cudaMemcpyAsync(h.skyview + c0, b.skyview + c0, cn * 8, cudaMemcpyDeviceToHost, s));
   } else {
-    HZ_CUDA(cudaMemcpyAsync(h.horizon, b.horizon, (size_t)h.num_hori * nc * 8,
-                            cudaMemcpyDeviceToHost, s));
-    HZ_CUDA(cudaMemcpyAsync(h.skyview, b.skyview, nc * 8, cudaMemcpyDeviceToHost, s));
+    HZ_CUDA(copy_to_host(E.staging, h.horizon, b.horizon, (size_t)h.num_hori * nc * 8, s));
+    HZ_CUDA(copy_to_host(E.staging, h.skyview, b.skyview, nc * 8, s));
   }
   return HZ_OK;
 }
@@ -817,11 +819,13 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
   const BatchBuffers bb = carve_batch(c, n, total_cells);
 
   std::vector<Problem> pr(n);
-  if (!on_device) HZ_CUDA(cudaEventRecord(E->ev[4], s));
+  // Host <-> device phases are timed on the host: pageable buffers are
+  // copied partly by host threads.
+  const auto t_h2d = std::chrono::steady_clock::now();
   for (int d = 0; d < n; d++) {
     const hz_domain& h = doms[d];
     if (!on_device) {
-      rc = stage_inputs(h, b[d], s);
+      rc = stage_inputs(*E, h, b[d], s);
       if (rc) return rc;
     }
     Problem& P = pr[d];
@@ -844,28 +848,31 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
     rc = cell_range(opt, h.num_cell, &P.cell_begin, &P.cell_count);
     if (rc) return rc;
   }
-  if (!on_device) HZ_CUDA(cudaEventRecord(E->ev[5], s));
+  double ms_h2d = 0.0;
+  if (!on_device) {
+    HZ_CUDA(cudaStreamSynchronize(s));
+    ms_h2d = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_h2d)
+                 .count();
+  }
   if (stats) std::memset(stats, 0, sizeof(*stats));
   RunOut out;
   rc = run_batch(*E, pr.data(), b.data(), n, bb, s, opt, stats, Stop::kFull, &out);
   if (rc) return rc;
   for (int d = 0; d < n; d++) doms[d].latency_ms = out.latency_ms[d];
+  const auto t_d2h = std::chrono::steady_clock::now();
   if (!on_device) {
-    HZ_CUDA(cudaEventRecord(E->ev[6], s));
     for (int d = 0; d < n; d++) {
-      rc = unstage_outputs(doms[d], b[d], pr[d].cell_begin, pr[d].cell_count, s);
+      rc = unstage_outputs(*E, doms[d], b[d], pr[d].cell_begin, pr[d].cell_count, s);
       if (rc) return rc;
     }
-    HZ_CUDA(cudaEventRecord(E->ev[7], s));
   }
   HZ_CUDA(cudaStreamSynchronize(s));
   if (stats) {
     if (!on_device) {
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, E->ev[4], E->ev[5]);
-      stats->ms_h2d = ms;
-      cudaEventElapsedTime(&ms, E->ev[6], E->ev[7]);
-      stats->ms_d2h = ms;
+      stats->ms_h2d = ms_h2d;
+      stats->ms_d2h =
+          std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_d2h)
+              .count();
     }
     stats->ms_total =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -1077,7 +1084,7 @@ static int mesh_host_common(const double* clon, const double* clat, const double
   const BatchBuffers bb = carve_batch(c, 1, num_cell);
   hz_domain h = make_domain(clon, clat, hsurf, vlon, vlat, cov, nullptr, nullptr, num_cell,
                             num_vertex, 4, grid_type, 1e4, 1.0, 1, 0);
-  rc = stage_inputs(h, b, s);
+  rc = stage_inputs(*E, h, b, s);
   if (rc) return rc;
   Problem pr;
   std::memset(&pr, 0, sizeof(pr));

@@ -173,6 +173,18 @@ cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, i
                        int* work, unsigned long long* counters, int* err, const TraceKnobs& k,
                        bool count_work, bool precise, cudaStream_t s);
 
+// ---- hz_hostcopy.cu ---------------------------------------------------------
+// Copies between device memory and caller host buffers: page-locked buffers
+// by cudaMemcpyAsync (asynchronous), pageable ones through two page-locked
+// chunks with multi-threaded host copies (returns when the data has arrived).
+struct Staging;
+cudaError_t staging_create(Staging** out);
+void staging_destroy(Staging* st);
+cudaError_t copy_to_host(Staging* st, void* dst, const void* src_dev, size_t bytes,
+                         cudaStream_t s);
+cudaError_t copy_from_host(Staging* st, void* dst_dev, const void* src, size_t bytes,
+                           cudaStream_t s);
+
 // ---- hz_learn.cu ------------------------------------------------------------
 constexpr int kMlpIn = 32;
 constexpr int kMlpHidden = 64;

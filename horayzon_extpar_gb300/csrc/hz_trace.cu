@@ -359,8 +359,19 @@ constexpr int kFlatBlock = 128;
 #define HZ_WARP_MIN_BLOCKS 6  // resident blocks per SM the register budget targets
 #endif
 
+#ifndef HZ_PREFETCH
+#define HZ_PREFETCH 1  // 1: prefetch the next node / postponed leaf into L1
+#endif
+// L1 prefetch of one 128-byte line (a hint: no fault on any address the
+// kernel would load itself).
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+#if HZ_PREFETCH
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+#endif
+}
+
 #ifndef HZ_NODE_STEPS
-#define HZ_NODE_STEPS 1  // node visits per lane in one node pass
+#define HZ_NODE_STEPS 2  // node visits per lane in one node pass
 #endif
 #ifndef HZ_NODE4_ORDER
 #define HZ_NODE4_ORDER 0  // 0: hit children sorted by entry distance; 1: nearest first only
@@ -446,6 +457,7 @@ __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, co
   if (t2 != INFINITY) stack[sp++] = r2;
   if (t1 != INFINITY) stack[sp++] = r1;
   ref = r0;
+  if (ref >= 0) prefetch_l1(nodes4 + ref);
   return true;
 }
 
@@ -514,7 +526,9 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   auto settle = [&]() {
     if (ref < 0 && ref != kEmptyRef && pl0 == 0) {
       pl0 = (leaf_start(ref) << 4) | leaf_count(ref);
+      prefetch_l1(tris + leaf_start(ref));
       ref = sp > 0 ? stack[--sp] : kEmptyRef;
+      if (kWide && ref >= 0) prefetch_l1(nodes4 + ref);
     }
     if (ref == kEmptyRef && pl0 == 0) {
       need = true;
