@@ -386,6 +386,9 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   for (int d = 0; d < n; d++) HZ_CUDA(cudaMemsetAsync(b[d].err, 0, 4 * sizeof(int), s));
   HZ_CUDA(cudaMemsetAsync(bb.err, 0, 4 * sizeof(int), s));
   HZ_CUDA(cudaMemsetAsync(bb.counters, 0, kCounterWords * sizeof(unsigned long long), s));
+#ifdef HZ_DIAG
+  HZ_CUDA(cudaMemsetAsync(bb.counters + 12, 0xFF, 2 * sizeof(unsigned long long), s));
+#endif
   HZ_CUDA(cudaMemsetAsync(bb.done, 0, 2 * sizeof(unsigned long long) * (size_t)n, s));
   HZ_CUDA(cudaEventRecord(E.ev[0], s));
 

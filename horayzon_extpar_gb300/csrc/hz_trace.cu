@@ -359,17 +359,6 @@ constexpr int kFlatBlock = 128;
 #define HZ_WARP_MIN_BLOCKS 6  // resident blocks per SM the register budget targets
 #endif
 
-#ifndef HZ_PREFETCH
-#define HZ_PREFETCH 1  // 1: prefetch the next node / postponed leaf into L1
-#endif
-// L1 prefetch of one 128-byte line (a hint: no fault on any address the
-// kernel would load itself).
-__device__ __forceinline__ void prefetch_l1(const void* p) {
-#if HZ_PREFETCH
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-#endif
-}
-
 #ifndef HZ_NODE_STEPS
 #define HZ_NODE_STEPS 2  // node visits per lane in one node pass
 #endif
@@ -457,7 +446,6 @@ __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, co
   if (t2 != INFINITY) stack[sp++] = r2;
   if (t1 != INFINITY) stack[sp++] = r1;
   ref = r0;
-  if (ref >= 0) prefetch_l1(nodes4 + ref);
   return true;
 }
 
@@ -516,8 +504,10 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
 #ifdef HZ_DIAG
   // Per-warp loop statistics: iterations, node passes, node lanes, triangle
   // passes, triangle lanes, advance passes, advancing lanes, live lanes,
-  // tracing lanes (summed over iterations).
+  // tracing lanes (summed over iterations); warp start / end times.
   unsigned long long dg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned long long t_start;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
 #endif
 
   // A leaf target is postponed when the lane holds none and the lane
@@ -526,9 +516,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   auto settle = [&]() {
     if (ref < 0 && ref != kEmptyRef && pl0 == 0) {
       pl0 = (leaf_start(ref) << 4) | leaf_count(ref);
-      prefetch_l1(tris + leaf_start(ref));
       ref = sp > 0 ? stack[--sp] : kEmptyRef;
-      if (kWide && ref >= 0) prefetch_l1(nodes4 + ref);
     }
     if (ref == kEmptyRef && pl0 == 0) {
       need = true;
@@ -802,6 +790,12 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     }
 #ifdef HZ_DIAG
     for (int q = 0; q < 9; q++) atomicAdd(&counters[3 + q], dg[q]);
+    unsigned long long t_end;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
+    atomicMin(&counters[12], t_start);  // host clears this word to ~0
+    atomicMin(&counters[13], t_end);
+    atomicMax(&counters[14], t_end);
+    atomicAdd(&counters[15], t_end - t_start);
 #endif
   }
 }
