@@ -296,6 +296,24 @@ def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args):
     return out
 
 
+def drop_in_report(dom, steps):
+    """The Python drop-in (horizon_svf_comp_py) on ordinary numpy arrays, as a
+    user of the reference calls it: pageable host buffers, wall clock."""
+    from horayzon_extpar_gb300 import horizon_svf_comp_py
+    inputs = [np.ascontiguousarray(a) for a in dom.inputs()]
+    horizon_svf_comp_py(*inputs, *ARGS)  # warm-up
+    walls, st = [], None
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        _, _, st = horizon_svf_comp_py(*inputs, *ARGS, return_stats=True)
+        walls.append(time.perf_counter() - t0)
+    w = float(np.median(walls))
+    return {"call": "horizon_svf_comp_py(numpy arrays)", "value": dom.ncell * ARGS[0] / w,
+            "unit": "evals/s", "wall_ms": 1e3 * w,
+            "phase_ms": {k: st[k] for k in ("ms_h2d", "ms_mesh", "ms_bvh", "ms_trace",
+                                              "ms_d2h")}}
+
+
 def batch_report(args):
     """64 uneven independent domains in one call (one persistent search)."""
     from horayzon_extpar_gb300 import synthetic
@@ -464,6 +482,7 @@ def run_gpu(args):
         extras["learned"] = learned_report(dom, d_in, hz, sv, stream, ms, args)
         extras["precision"] = precision_report(dom, d_in, hz, sv, stream)
         extras["batched_domains"] = batch_report(args)
+        extras["drop_in_numpy"] = drop_in_report(dom, min(args.steps, 3))
 
     peak, peak_kind = measured_peaks()
     alg_bytes = BYTES_PER_NODE * st_count["node_visits"] + BYTES_PER_TRI * st_count["tri_tests"]

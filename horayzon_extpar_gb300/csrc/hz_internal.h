@@ -167,7 +167,7 @@ struct TraceKnobs {
   int advance_min;  // 1..32
   int leaf_min;     // 1..32
   int chunk;        // work ids a warp claims per atomic (< 1: kDefaultChunk)
-  int variant;      // kTraceWide / kTraceBinary
+  int variant;      // kTrace*
 };
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
                        int* work, unsigned long long* counters, int* err, const TraceKnobs& k,

@@ -465,6 +465,185 @@ __device__ __forceinline__ bool test_tri(const Tri* __restrict__ tris,
   return tri_hit(r, v0, v1, v2);
 }
 
+// One step of a cell's bracketing search (mo_lradtopo_horayzon.cpp:490-555,
+// 694-754) on the state `st` (FP64: 0-2 sphere normal U, 3-5 north N, 6-8
+// east E, 9-11 horizontal direction of the current azimuth, 12 elevation
+// accumulator, 13 sector sum, 14 SVF sum; integers: domain, cell, azimuth,
+// phase, upward steps, lattice index m; FP32 ray origin hi and lo). Given the
+// result of the cell's last ray (or, in phase kPhaseStart, the work id k_new
+// of a new cell), it continues the bracket, or closes the azimuth (clip,
+// sector mean, SVF) and starts the next one, or finishes the cell. Returns 1
+// with the next ray's direction, 0 when the cell has finished (the state is
+// back in kPhaseStart and needs a new work id), -1 when k_new is past the
+// last work id.
+template <bool kPrecise, class S>
+__device__ __forceinline__ int search_step(const S& st, const DomainDesc* __restrict__ doms,
+                                           int ndom, const int* __restrict__ order, int total,
+                                           int k_new, bool last_hit, float3& dir, int& dom_out) {
+#define SV(k_) st.d(k_)
+#define SO(k_) st.f(k_)
+  int dom = st.i(0), cell = st.i(1), a = st.i(2), phase = st.i(3), up = st.i(4), m = st.i(5);
+  bool alive = true;
+  bool emit = false;
+  while (!emit) {
+    if (phase == kPhaseStart) {
+      const int k = k_new;
+      if (k >= total) {
+        alive = false;
+        break;
+      }
+      const long long g = order[k];
+      int lo = 0, hi = ndom - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (doms[mid].cell_offset <= g) lo = mid;
+        else hi = mid - 1;
+      }
+      dom = lo;
+      const DomainDesc& D = doms[dom];
+      cell = (int)(g - D.cell_offset);
+      // Cell frame, mo_lradtopo_horayzon.cpp:694-720.
+      const V3 q{D.cell_enu[3LL * cell], D.cell_enu[3LL * cell + 1],
+                 D.cell_enu[3LL * cell + 2]};
+      V3 normal{q.x - D.centre.x, q.y - D.centre.y, q.z - D.centre.z};
+      unit3(normal);
+      const V3 v_n{D.pole.x - q.x, D.pole.y - q.y, D.pole.z - q.z};
+      const double dp = dot3(v_n, normal);
+      V3 north{v_n.x - dp * normal.x, v_n.y - dp * normal.y, v_n.z - dp * normal.z};
+      unit3(north);
+      const V3 east = cross3(north, normal);
+      const double o64x = q.x + normal.x * D.ray_org_elev;
+      const double o64y = q.y + normal.y * D.ray_org_elev;
+      const double o64z = q.z + normal.z * D.ray_org_elev;
+      const float ox = (float)o64x, oy = (float)o64y, oz = (float)o64z;
+      SO(0) = ox;
+      SO(1) = oy;
+      SO(2) = oz;
+      if (kPrecise) {
+        SO(3) = (float)(o64x - (double)ox);
+        SO(4) = (float)(o64y - (double)oy);
+        SO(5) = (float)(o64z - (double)oz);
+      }
+      SV(0) = normal.x; SV(1) = normal.y; SV(2) = normal.z;
+      SV(3) = north.x; SV(4) = north.y; SV(5) = north.z;
+      SV(6) = east.x; SV(7) = east.y; SV(8) = east.z;
+      SV(12) = 0.0; SV(13) = 0.0; SV(14) = 0.0;
+      a = 0;
+      m = 0;
+      phase = kPhaseFirst;
+    } else {
+      // Result of the last ray: continue the bracket or close the azimuth.
+      const DomainDesc& D = doms[dom];
+      const double ha = D.hori_acc;
+      double elev = SV(12);
+      if (phase == kPhaseFirst) {
+        phase = last_hit ? kPhaseUp : kPhaseDown;
+        up = 0;
+      }
+      const bool step_up = phase == kPhaseUp && last_hit && up < kMaxUpSteps;
+      const bool step_dn = phase == kPhaseDown && !last_hit && elev > D.elev_floor;
+      if (step_up || step_dn) {
+        if (step_up) {
+          up++;
+          m++;
+          elev += (2.0 * ha);
+        } else {
+          m--;
+          elev -= (2.0 * ha);
+        }
+        SV(12) = elev;
+        emit = true;
+        break;
+      }
+      // cpp:535/546, then the clip / sector / SVF epilogue of cpp:736-754.
+      double h = phase == kPhaseUp ? elev - ha : elev + ha;
+      const int j = phase == kPhaseUp ? 2 * m - 1 : 2 * m + 1;  // h ~ j * ha
+      if (D.raw_j) D.raw_j[(long long)a * D.ncell + cell] = (int16_t)j;
+      if (h < 0.0) h = 0.0;
+      double sector = SV(13) + h;
+      if ((a + 1) % D.refine == 0) {
+        // x / 1.0 == x exactly, so the division is skipped for refine 1.
+        const double deg = (sector / kPi) * 180.0;
+        D.horizon[(long long)(a / D.refine) * D.ncell + cell] =
+            D.refine == 1 ? deg : deg / (double)D.refine;
+        sector = 0.0;
+      }
+      double s = 0.0;
+      if (h > 0.0) s = (j > 0 && j < kSinTable) ? __ldg(&D.sin_lattice[j]) : sin(h);
+      double svf = SV(14);
+      if (D.svf_type == 0) svf += (1.0 - s);
+      else if (D.svf_type == 1) svf += (1.0 - (s * s));
+      else svf += (1.0 - (s * s * s));
+      a++;
+      if (a == D.L) {
+        D.skyview[cell] = svf / (double)D.L;
+        if (D.done) {
+          // Completion time of the domain's last cell (batch latency).
+          const unsigned long long fin_cells = atomicAdd(&D.done[0], 1ull) + 1ull;
+          if (fin_cells == (unsigned long long)D.ncell_traced) {
+            unsigned long long now;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+            D.done[1] = now;
+          }
+        }
+        // The next cell comes from the warp's chunk in the next pass.
+        phase = kPhaseStart;
+        break;
+      }
+      SV(13) = sector;
+      SV(14) = svf;
+      phase = kPhaseFirst;
+    }
+    // New azimuth: the elevation carries over (cpp:511), or starts at the
+    // learned proposal; horizontal direction cos(theta_a) N + sin(theta_a) E.
+    const int16_t* start_m = doms[dom].start_m;
+    if (start_m && (a == 0 || doms[dom].start_all)) {
+      m = start_m[(long long)a * doms[dom].ncell + cell];
+      SV(12) = (double)m * (2.0 * doms[dom].hori_acc);
+    }
+    const double2 cs = __ldg(&doms[dom].azim_cs[a]);
+    SV(9) = cs.x * SV(3) + cs.y * SV(6);
+    SV(10) = cs.x * SV(4) + cs.y * SV(7);
+    SV(11) = cs.x * SV(5) + cs.y * SV(8);
+    emit = true;
+  }
+  st.i(3) = phase;
+  if (!alive) return -1;
+  if (!emit) return 0;
+  st.i(0) = dom;
+  st.i(1) = cell;
+  st.i(2) = a;
+  st.i(4) = up;
+  st.i(5) = m;
+  // Direction at lattice elevation m: cos(e_m) h_a + sin(e_m) U.
+  const DomainDesc& D = doms[dom];
+  double2 ecs;
+  if (m >= kElevMin && m < kElevMin + kElevTable) {
+    ecs = __ldg(&D.elev_cs[m - kElevMin]);
+  } else {
+    const double e = (double)m * (2.0 * D.hori_acc);
+    ecs = make_double2(cos(e), sin(e));
+  }
+  dir.x = (float)(ecs.x * SV(9) + ecs.y * SV(0));
+  dir.y = (float)(ecs.x * SV(10) + ecs.y * SV(1));
+  dir.z = (float)(ecs.x * SV(11) + ecs.y * SV(2));
+  dom_out = dom;
+  return 1;
+#undef SV
+#undef SO
+}
+
+// Search state of one lane in shared memory (k_trace_warp).
+struct LaneState {
+  double (*sv)[kFlatBlock];
+  int (*si)[kFlatBlock];
+  float (*so)[kFlatBlock];
+  int t;
+  __device__ double& d(int f) const { return sv[f][t]; }
+  __device__ int& i(int f) const { return si[f][t]; }
+  __device__ float& f(int k) const { return so[k][t]; }
+};
+
 template <bool kCount, bool kPrecise, bool kWide>
 __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     k_trace_warp(const DomainDesc* __restrict__ doms, int ndom, const int* __restrict__ order,
@@ -566,159 +745,23 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
       }
     }
     if (advance && alive && need) {
-      int dom = si[0][t], cell = si[1][t], a = si[2][t], phase = si[3][t], up = si[4][t];
-      int m = si[5][t];
-      bool emit = false;
-      while (!emit) {
-        if (phase == kPhaseStart) {
-          const int k = k_new;
-          if (k >= total) {
-            alive = false;
-            break;
-          }
-          const long long g = order[k];
-          int lo = 0, hi = ndom - 1;
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (doms[mid].cell_offset <= g) lo = mid;
-            else hi = mid - 1;
-          }
-          dom = lo;
-          const DomainDesc& D = doms[dom];
-          cell = (int)(g - D.cell_offset);
-          // Cell frame, mo_lradtopo_horayzon.cpp:694-720.
-          const V3 q{D.cell_enu[3LL * cell], D.cell_enu[3LL * cell + 1],
-                     D.cell_enu[3LL * cell + 2]};
-          V3 normal{q.x - D.centre.x, q.y - D.centre.y, q.z - D.centre.z};
-          unit3(normal);
-          const V3 v_n{D.pole.x - q.x, D.pole.y - q.y, D.pole.z - q.z};
-          const double dp = dot3(v_n, normal);
-          V3 north{v_n.x - dp * normal.x, v_n.y - dp * normal.y, v_n.z - dp * normal.z};
-          unit3(north);
-          const V3 east = cross3(north, normal);
-          const double o64x = q.x + normal.x * D.ray_org_elev;
-          const double o64y = q.y + normal.y * D.ray_org_elev;
-          const double o64z = q.z + normal.z * D.ray_org_elev;
-          const float ox = (float)o64x, oy = (float)o64y, oz = (float)o64z;
-          so[0][t] = ox;
-          so[1][t] = oy;
-          so[2][t] = oz;
-          if (kPrecise) {
-            so[3][t] = (float)(o64x - (double)ox);
-            so[4][t] = (float)(o64y - (double)oy);
-            so[5][t] = (float)(o64z - (double)oz);
-          }
-          sv[0][t] = normal.x; sv[1][t] = normal.y; sv[2][t] = normal.z;
-          sv[3][t] = north.x; sv[4][t] = north.y; sv[5][t] = north.z;
-          sv[6][t] = east.x; sv[7][t] = east.y; sv[8][t] = east.z;
-          sv[12][t] = 0.0; sv[13][t] = 0.0; sv[14][t] = 0.0;
-          a = 0;
-          m = 0;
-          phase = kPhaseFirst;
-        } else {
-          // Result of the last ray: continue the bracket or close the azimuth.
-          const DomainDesc& D = doms[dom];
-          const double ha = D.hori_acc;
-          double elev = sv[12][t];
-          if (phase == kPhaseFirst) {
-            phase = last_hit ? kPhaseUp : kPhaseDown;
-            up = 0;
-          }
-          const bool step_up = phase == kPhaseUp && last_hit && up < kMaxUpSteps;
-          const bool step_dn = phase == kPhaseDown && !last_hit && elev > D.elev_floor;
-          if (step_up || step_dn) {
-            if (step_up) {
-              up++;
-              m++;
-              elev += (2.0 * ha);
-            } else {
-              m--;
-              elev -= (2.0 * ha);
-            }
-            sv[12][t] = elev;
-            emit = true;
-            break;
-          }
-          // cpp:535/546, then the clip / sector / SVF epilogue of cpp:736-754.
-          double h = phase == kPhaseUp ? elev - ha : elev + ha;
-          const int j = phase == kPhaseUp ? 2 * m - 1 : 2 * m + 1;  // h ~ j * ha
-          if (D.raw_j) D.raw_j[(long long)a * D.ncell + cell] = (int16_t)j;
-          if (h < 0.0) h = 0.0;
-          double sector = sv[13][t] + h;
-          if ((a + 1) % D.refine == 0) {
-            // x / 1.0 == x exactly, so the division is skipped for refine 1.
-            const double deg = (sector / kPi) * 180.0;
-            D.horizon[(long long)(a / D.refine) * D.ncell + cell] =
-                D.refine == 1 ? deg : deg / (double)D.refine;
-            sector = 0.0;
-          }
-          double s = 0.0;
-          if (h > 0.0) s = (j > 0 && j < kSinTable) ? __ldg(&D.sin_lattice[j]) : sin(h);
-          double svf = sv[14][t];
-          if (D.svf_type == 0) svf += (1.0 - s);
-          else if (D.svf_type == 1) svf += (1.0 - (s * s));
-          else svf += (1.0 - (s * s * s));
-          a++;
-          if (a == D.L) {
-            D.skyview[cell] = svf / (double)D.L;
-            if (D.done) {
-              // Completion time of the domain's last cell (batch latency).
-              const unsigned long long fin_cells = atomicAdd(&D.done[0], 1ull) + 1ull;
-              if (fin_cells == (unsigned long long)D.ncell_traced) {
-                unsigned long long now;
-                asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
-                D.done[1] = now;
-              }
-            }
-            // The next cell comes from the warp's chunk in the next pass.
-            phase = kPhaseStart;
-            break;
-          }
-          sv[13][t] = sector;
-          sv[14][t] = svf;
-          phase = kPhaseFirst;
-        }
-        // New azimuth: the elevation carries over (cpp:511), or starts at the
-        // learned proposal; horizontal direction cos(theta_a) N + sin(theta_a) E.
-        const int16_t* start_m = doms[dom].start_m;
-        if (start_m && (a == 0 || doms[dom].start_all)) {
-          m = start_m[(long long)a * doms[dom].ncell + cell];
-          sv[12][t] = (double)m * (2.0 * doms[dom].hori_acc);
-        }
-        const double2 cs = __ldg(&doms[dom].azim_cs[a]);
-        sv[9][t] = cs.x * sv[3][t] + cs.y * sv[6][t];
-        sv[10][t] = cs.x * sv[4][t] + cs.y * sv[7][t];
-        sv[11][t] = cs.x * sv[5][t] + cs.y * sv[8][t];
-        emit = true;
-      }
-      si[3][t] = phase;
-      if (alive && emit) {
-        si[0][t] = dom;
-        si[1][t] = cell;
-        si[2][t] = a;
-        si[4][t] = up;
-        si[5][t] = m;
+      const LaneState st{sv, si, so, t};
+      float3 d;
+      int dom = 0;
+      const int res = search_step<kPrecise>(st, doms, ndom, order, total, k_new, last_hit, d, dom);
+      if (res < 0) {
+        alive = false;
+      } else if (res > 0) {
         const DomainDesc& D = doms[dom];
         if (kWide) nodes4 = D.nodes4;
         else nodes = D.nodes;
         tris = D.tris;
         if (kPrecise) tri_lo = D.tri_lo;
-        // Direction at lattice elevation m: cos(e_m) h_a + sin(e_m) U.
-        double2 ecs;
-        if (m >= kElevMin && m < kElevMin + kElevTable) {
-          ecs = __ldg(&D.elev_cs[m - kElevMin]);
-        } else {
-          const double e = (double)m * (2.0 * D.hori_acc);
-          ecs = make_double2(cos(e), sin(e));
-        }
-        const float dx = (float)(ecs.x * sv[9][t] + ecs.y * sv[0][t]);
-        const float dy = (float)(ecs.x * sv[10][t] + ecs.y * sv[1][t]);
-        const float dz = (float)(ecs.x * sv[11][t] + ecs.y * sv[2][t]);
         if (kPrecise)
-          r = make_ray(so[0][t], so[1][t], so[2][t], dx, dy, dz, D.tfar, so[3][t], so[4][t],
+          r = make_ray(so[0][t], so[1][t], so[2][t], d.x, d.y, d.z, D.tfar, so[3][t], so[4][t],
                        so[5][t]);
         else
-          r = make_ray(so[0][t], so[1][t], so[2][t], dx, dy, dz, D.tfar);
+          r = make_ray(so[0][t], so[1][t], so[2][t], d.x, d.y, d.z, D.tfar);
         ref = D.root;
         sp = 0;
         pl0 = 0;

@@ -279,3 +279,4 @@ def test_gpu_queue_chunk_keeps_results(small_domain, queue_chunk):
     np.testing.assert_array_equal(h0, h1)
     np.testing.assert_array_equal(s0, s1)
     assert st0["num_rays"] == st1["num_rays"]
+
