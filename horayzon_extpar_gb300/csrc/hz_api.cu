@@ -107,6 +107,8 @@ struct Buffers {
   long long raster_budget;
   int16_t* start_m;
   double* cell_enu;
+  double* cell_frame;  // [9][ncell] (persistent search)
+  float* cell_origin;  // [6][ncell]
   // BVH
   Node* nodes;
   Node4* nodes4;     // wide traversal only
@@ -157,6 +159,8 @@ Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhor
   b.origin_sum = c.take<double>(4);
   b.vert32 = c.take<float>(3 * max_mv);
   b.cell_enu = c.take<double>(3 * ncell);
+  b.cell_frame = c.take<double>(9 * ncell);
+  b.cell_origin = c.take<float>(6 * ncell);
   const long long nt = max_tri > 0 ? max_tri : 1;
   b.nodes = c.take<Node>(nt > 1 ? nt - 1 : 1);
   if (wide) b.nodes4 = c.take<Node4>(nt > 1 ? nt - 1 : 1);
@@ -579,6 +583,8 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       DomainDesc D;
       std::memset(&D, 0, sizeof(D));
       D.cell_enu = b[d].cell_enu;
+      D.cell_frame = b[d].cell_frame;
+      D.cell_origin = b[d].cell_origin;
       D.nodes = b[d].nodes;
       D.nodes4 = b[d].nodes4;
       D.tris = b[d].tris;

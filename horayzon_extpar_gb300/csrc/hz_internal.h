@@ -125,12 +125,15 @@ cudaError_t cell_order(const double* cell_enu, int begin, int count, int id_offs
 // One domain of the persistent search (device-resident array).
 struct DomainDesc {
   const double* cell_enu;     // [3 * ncell] FP64 ENU of cell centres
+  double* cell_frame;         // [9][ncell] sphere normal, north, east (k_cell_frames)
+  float* cell_origin;         // [6][ncell] FP32 ray origin, precise mode: + residual
   const Node* nodes;
   const Node4* nodes4;        // BVH4 collapse of nodes (wide traversal only)
   const Tri* tris;
   const float4* tri_lo;       // precise mode: [3 * n_tri] FP32 vertex residuals
-  double* horizon;            // [nhori * ncell] degrees
-  double* skyview;            // [ncell]
+  double* horizon;            // [nhori * ncell] degrees (the search leaves the sector
+                              // sums in radians; k_finish_outputs converts them)
+  double* skyview;            // [ncell] (the search leaves the sums over azimuths)
   const double2* azim_cs;     // lattice tables (trace_tables)
   const double2* elev_cs;
   const double* sin_lattice;
@@ -147,7 +150,9 @@ struct DomainDesc {
 
 // Persistent flattened search (same rays and results as trace_exact) over
 // `total` work ids from `order`; a work id is cell_offset + cell of its
-// domain, and `doms` is sorted by cell_offset.
+// domain, and `doms` is sorted by cell_offset. Three launches: the cell
+// frames of every traced cell (FP64, coalesced), the search, and the
+// conversion of the accumulated sums into degrees and SVF.
 // precise: every domain carries tri_lo and rays use hi + lo vertices/origin.
 // k.variant: the BVH the search traverses (kTrace*); k.advance_min /
 // k.leaf_min: lanes of a warp that must be waiting before the search state

@@ -70,7 +70,8 @@ struct Layout {
 struct StaticBuffers {
   unsigned long long *packed, *offsets, *scan_partials, *totals;
   int* vot;
-  double *add_lon, *add_lat, *add_h, *ecef, *block_sums, *origin_sum, *cell_enu;
+  double *add_lon, *add_lat, *add_h, *ecef, *block_sums, *origin_sum, *cell_enu, *cell_frame;
+  float* cell_origin;
   float* vert32;
   Node* nodes;
   Tri* tris;
@@ -105,6 +106,8 @@ StaticBuffers lay_out(Layout& L, long long ncell, long long nvert, long long max
   b.origin_sum = L.take<double>(4);
   b.vert32 = L.take<float>(3 * max_mv);
   b.cell_enu = L.take<double>(3 * ncell);
+  b.cell_frame = L.take<double>(9 * ncell);
+  b.cell_origin = L.take<float>(6 * ncell);
   b.nodes = L.take<Node>(nt > 1 ? nt - 1 : 1);
   b.tris = L.take<Tri>(nt);
   b.bvh.keys = L.take<uint32_t>(nt);
@@ -198,7 +201,7 @@ extern "C" int hz_horizon_svf_device_static(
     char buf[320];
     snprintf(buf, sizeof(buf),
              "domain needs %zu bytes of scratch, above the fixed %zu-byte static array "
-             "(about 100,000 cells); use hz_horizon_svf_device",
+             "(about 90,000 cells); use hz_horizon_svf_device",
              dry.off, kStaticScratchBytes);
     set_last_error(buf);
     return HZ_ERR_VALUE;
@@ -265,6 +268,8 @@ extern "C" int hz_horizon_svf_device_static(
   DomainDesc D;
   std::memset(&D, 0, sizeof(D));
   D.cell_enu = b.cell_enu;
+  D.cell_frame = b.cell_frame;
+  D.cell_origin = b.cell_origin;
   D.nodes = b.nodes;
   D.tris = b.tris;
   D.horizon = horizon;

@@ -465,6 +465,18 @@ __device__ __forceinline__ bool test_tri(const Tri* __restrict__ tris,
   return tri_hit(r, v0, v1, v2);
 }
 
+// Domain of work id g (doms sorted by cell_offset).
+__device__ __forceinline__ int domain_of(const DomainDesc* __restrict__ doms, int ndom,
+                                         long long g) {
+  int lo = 0, hi = ndom - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (doms[mid].cell_offset <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 // One step of a cell's bracketing search (mo_lradtopo_horayzon.cpp:490-555,
 // 694-754) on the state `st` (FP64: 0-2 sphere normal U, 3-5 north N, 6-8
 // east E, 9-11 horizontal direction of the current azimuth, 12 elevation
@@ -493,40 +505,24 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
         break;
       }
       const long long g = order[k];
-      int lo = 0, hi = ndom - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (doms[mid].cell_offset <= g) lo = mid;
-        else hi = mid - 1;
-      }
-      dom = lo;
+      dom = domain_of(doms, ndom, g);
       const DomainDesc& D = doms[dom];
       cell = (int)(g - D.cell_offset);
-      // Cell frame, mo_lradtopo_horayzon.cpp:694-720.
-      const V3 q{D.cell_enu[3LL * cell], D.cell_enu[3LL * cell + 1],
-                 D.cell_enu[3LL * cell + 2]};
-      V3 normal{q.x - D.centre.x, q.y - D.centre.y, q.z - D.centre.z};
-      unit3(normal);
-      const V3 v_n{D.pole.x - q.x, D.pole.y - q.y, D.pole.z - q.z};
-      const double dp = dot3(v_n, normal);
-      V3 north{v_n.x - dp * normal.x, v_n.y - dp * normal.y, v_n.z - dp * normal.z};
-      unit3(north);
-      const V3 east = cross3(north, normal);
-      const double o64x = q.x + normal.x * D.ray_org_elev;
-      const double o64y = q.y + normal.y * D.ray_org_elev;
-      const double o64z = q.z + normal.z * D.ray_org_elev;
-      const float ox = (float)o64x, oy = (float)o64y, oz = (float)o64z;
-      SO(0) = ox;
-      SO(1) = oy;
-      SO(2) = oz;
+      // Cell frame (mo_lradtopo_horayzon.cpp:694-720) from k_cell_frames.
+      const long long nc = D.ncell;
+      const double* fr = D.cell_frame + cell;
+      SV(0) = fr[0]; SV(1) = fr[nc]; SV(2) = fr[2 * nc];
+      SV(3) = fr[3 * nc]; SV(4) = fr[4 * nc]; SV(5) = fr[5 * nc];
+      SV(6) = fr[6 * nc]; SV(7) = fr[7 * nc]; SV(8) = fr[8 * nc];
+      const float* org = D.cell_origin + cell;
+      SO(0) = org[0];
+      SO(1) = org[nc];
+      SO(2) = org[2 * nc];
       if (kPrecise) {
-        SO(3) = (float)(o64x - (double)ox);
-        SO(4) = (float)(o64y - (double)oy);
-        SO(5) = (float)(o64z - (double)oz);
+        SO(3) = org[3 * nc];
+        SO(4) = org[4 * nc];
+        SO(5) = org[5 * nc];
       }
-      SV(0) = normal.x; SV(1) = normal.y; SV(2) = normal.z;
-      SV(3) = north.x; SV(4) = north.y; SV(5) = north.z;
-      SV(6) = east.x; SV(7) = east.y; SV(8) = east.z;
       SV(12) = 0.0; SV(13) = 0.0; SV(14) = 0.0;
       a = 0;
       m = 0;
@@ -562,10 +558,8 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       if (h < 0.0) h = 0.0;
       double sector = SV(13) + h;
       if ((a + 1) % D.refine == 0) {
-        // x / 1.0 == x exactly, so the division is skipped for refine 1.
-        const double deg = (sector / kPi) * 180.0;
-        D.horizon[(long long)(a / D.refine) * D.ncell + cell] =
-            D.refine == 1 ? deg : deg / (double)D.refine;
+        // Converted to degrees by k_finish_outputs.
+        D.horizon[(long long)(a / D.refine) * D.ncell + cell] = sector;
         sector = 0.0;
       }
       double s = 0.0;
@@ -576,7 +570,7 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       else svf += (1.0 - (s * s * s));
       a++;
       if (a == D.L) {
-        D.skyview[cell] = svf / (double)D.L;
+        D.skyview[cell] = svf;  // divided by L in k_finish_outputs
         if (D.done) {
           // Completion time of the domain's last cell (batch latency).
           const unsigned long long fin_cells = atomicAdd(&D.done[0], 1ull) + 1ull;
@@ -843,6 +837,62 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   }
 }
 
+// Frame and FP32 ray origin of every traced cell, mo_lradtopo_horayzon.cpp:
+// 694-720 (the per-cell kernel's expressions), as [9][ncell] / [6][ncell].
+template <bool kPrecise>
+__global__ void k_cell_frames(const DomainDesc* __restrict__ doms, int ndom,
+                              const int* __restrict__ order, int total) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= total) return;
+  const long long g = order[k];
+  const DomainDesc& D = doms[domain_of(doms, ndom, g)];
+  const int cell = (int)(g - D.cell_offset);
+  const V3 q{D.cell_enu[3LL * cell], D.cell_enu[3LL * cell + 1], D.cell_enu[3LL * cell + 2]};
+  V3 normal{q.x - D.centre.x, q.y - D.centre.y, q.z - D.centre.z};
+  unit3(normal);
+  const V3 v_n{D.pole.x - q.x, D.pole.y - q.y, D.pole.z - q.z};
+  const double dp = dot3(v_n, normal);
+  V3 north{v_n.x - dp * normal.x, v_n.y - dp * normal.y, v_n.z - dp * normal.z};
+  unit3(north);
+  const V3 east = cross3(north, normal);
+  const double o64x = q.x + normal.x * D.ray_org_elev;
+  const double o64y = q.y + normal.y * D.ray_org_elev;
+  const double o64z = q.z + normal.z * D.ray_org_elev;
+  const long long nc = D.ncell;
+  double* fr = D.cell_frame + cell;
+  fr[0] = normal.x; fr[nc] = normal.y; fr[2 * nc] = normal.z;
+  fr[3 * nc] = north.x; fr[4 * nc] = north.y; fr[5 * nc] = north.z;
+  fr[6 * nc] = east.x; fr[7 * nc] = east.y; fr[8 * nc] = east.z;
+  float* org = D.cell_origin + cell;
+  const float ox = (float)o64x, oy = (float)o64y, oz = (float)o64z;
+  org[0] = ox;
+  org[nc] = oy;
+  org[2 * nc] = oz;
+  if (kPrecise) {
+    org[3 * nc] = (float)(o64x - (double)ox);
+    org[4 * nc] = (float)(o64y - (double)oy);
+    org[5 * nc] = (float)(o64z - (double)oz);
+  }
+}
+
+// The search's sums to outputs (cpp:736-754): horizon sector sums [rad] ->
+// degrees and mean over refine_factor; SVF sum -> mean over the azimuths.
+// x / 1.0 == x exactly, so that division is skipped for refine_factor 1.
+__global__ void k_finish_outputs(const DomainDesc* __restrict__ doms, int ndom,
+                                 const int* __restrict__ order, int total) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= total) return;
+  const long long g = order[k];
+  const DomainDesc& D = doms[domain_of(doms, ndom, g)];
+  const int cell = (int)(g - D.cell_offset);
+  for (int j = 0; j < D.nhori; j++) {
+    double* h = D.horizon + (long long)j * D.ncell + cell;
+    const double deg = (*h / kPi) * 180.0;
+    *h = D.refine == 1 ? deg : deg / (double)D.refine;
+  }
+  D.skyview[cell] = D.skyview[cell] / (double)D.L;
+}
+
 // Morton keys (2 x 16 bits) of the traced cells' horizontal ENU position.
 __global__ void k_cell_bounds(const double* __restrict__ cell_enu, int begin, int count,
                               unsigned* __restrict__ bounds) {
@@ -981,10 +1031,30 @@ cudaError_t launch_variant(const DomainDesc* doms, int ndom, const int32_t* orde
                            total, work, counters, err, advance_min, leaf_min, chunk);
 }
 
+static cudaError_t launch_search(const DomainDesc* doms, int ndom, const int32_t* order,
+                                 int total, int* work, unsigned long long* counters, int* err,
+                                 const TraceKnobs& k, bool count_work, bool precise,
+                                 cudaStream_t s);
+
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
                        int* work, unsigned long long* counters, int* err, const TraceKnobs& k,
                        bool count_work, bool precise, cudaStream_t s) {
   if (total <= 0 || ndom <= 0) return cudaSuccess;
+  if (precise) k_cell_frames<true><<<grid_for(total, 256), 256, 0, s>>>(doms, ndom, order, total);
+  else k_cell_frames<false><<<grid_for(total, 256), 256, 0, s>>>(doms, ndom, order, total);
+  note_launches(1);
+  cudaError_t e =
+      launch_search(doms, ndom, order, total, work, counters, err, k, count_work, precise, s);
+  if (e != cudaSuccess) return e;
+  k_finish_outputs<<<grid_for(total, 256), 256, 0, s>>>(doms, ndom, order, total);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_search(const DomainDesc* doms, int ndom, const int32_t* order,
+                                 int total, int* work, unsigned long long* counters, int* err,
+                                 const TraceKnobs& k, bool count_work, bool precise,
+                                 cudaStream_t s) {
   const int c = k.chunk >= 1 ? k.chunk : kDefaultChunk;
   if (precise)
     return count_work ? launch_variant<true, true>(doms, ndom, order, total, work, counters,

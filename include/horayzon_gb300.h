@@ -260,7 +260,7 @@ int hz_mesh_enu32(const double* clon, const double* clat, const double* hsurf,
  * cudaMalloc/cudaFree. It allocates nothing: all intermediate data lives in
  * one fixed 64 MiB __device__ array inside the library (held by every GPU
  * that loads it until the process exits), which limits a domain to about
- * 100,000 cells; larger domains are rejected with HZ_ERR_VALUE and a message
+ * 90,000 cells; larger domains are rejected with HZ_ERR_VALUE and a message
  * naming the limit. The first call on a device resolves the array's device
  * address (cudaGetSymbolAddress) with that device current; make that first
  * call before any stream capture. All calls share the array: calls whose GPU
