@@ -602,6 +602,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.pole = frames[d].pole;
       D.ray_org_elev = P.ray_org_elev;
       D.hori_acc = hori_acc;
+      D.two_ha = 2.0 * hori_acc;
       D.elev_floor = elev_floor;
       D.cell_offset = total - P.cell_begin;
       D.root = out->n_tri[d] > 0 ? 0 : kEmptyRef;

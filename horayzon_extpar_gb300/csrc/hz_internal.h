@@ -143,6 +143,7 @@ struct DomainDesc {
   int16_t* raw_j;             // optional output: unclipped horizon j (h = j * 0.25 deg)
   double3 centre, pole;       // Earth centre / North Pole in ENU
   double ray_org_elev, hori_acc, elev_floor;
+  double two_ha;              // 2 * hori_acc (exact): one elevation step
   long long cell_offset;      // work id of cell 0 of this domain
   int root, ncell, ncell_traced, nhori, refine, L, svf_type;
   float tfar;
@@ -165,7 +166,7 @@ enum : int {
 // Counter words of the search: 0 rays, 1 node visits, 2 triangle tests; with
 // -DHZ_DIAG, 3.. per-warp loop statistics (printed to stderr by the host).
 constexpr int kCounterWords = 16;
-constexpr int kDefaultAdvanceMin = 16;
+constexpr int kDefaultAdvanceMin = 12;
 constexpr int kDefaultLeafMin = 12;
 constexpr int kDefaultChunk = 32;
 struct TraceKnobs {

@@ -281,6 +281,7 @@ extern "C" int hz_horizon_svf_device_static(
   D.pole = fr.pole;
   D.ray_org_elev = ray_org_elev;
   D.hori_acc = deg2rad_s(0.25);
+  D.two_ha = 2.0 * D.hori_acc;
   D.elev_floor = deg2rad_s(-85.0);
   D.cell_offset = 0;
   D.root = n_tri > 0 ? 0 : kEmptyRef;

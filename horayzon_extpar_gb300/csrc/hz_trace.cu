@@ -465,6 +465,13 @@ __device__ __forceinline__ bool test_tri(const Tri* __restrict__ tris,
   return tri_hit(r, v0, v1, v2);
 }
 
+// One azimuth's SVF term for sin(h) = s (cpp:333-358).
+__device__ __forceinline__ double svf_term(double s, int svf_type) {
+  if (svf_type == 0) return 1.0 - s;
+  if (svf_type == 1) return 1.0 - (s * s);
+  return 1.0 - (s * s * s);
+}
+
 // Domain of work id g (doms sorted by cell_offset).
 __device__ __forceinline__ int domain_of(const DomainDesc* __restrict__ doms, int ndom,
                                          long long g) {
@@ -542,10 +549,10 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
         if (step_up) {
           up++;
           m++;
-          elev += (2.0 * ha);
+          elev += D.two_ha;
         } else {
           m--;
-          elev -= (2.0 * ha);
+          elev -= D.two_ha;
         }
         SV(12) = elev;
         emit = true;
@@ -557,20 +564,23 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       if (D.raw_j) D.raw_j[(long long)a * D.ncell + cell] = (int16_t)j;
       if (h < 0.0) h = 0.0;
       double sector = SV(13) + h;
-      if ((a + 1) % D.refine == 0) {
+      if (D.refine == 1 || (a + 1) % D.refine == 0) {
         // Converted to degrees by k_finish_outputs.
-        D.horizon[(long long)(a / D.refine) * D.ncell + cell] = sector;
+        D.horizon[(long long)(D.refine == 1 ? a : a / D.refine) * D.ncell + cell] = sector;
         sector = 0.0;
       }
-      double s = 0.0;
-      if (h > 0.0) s = (j > 0 && j < kSinTable) ? __ldg(&D.sin_lattice[j]) : sin(h);
+      // SVF sum (cpp:333-358, 754). With refine_factor 1 the horizon array
+      // holds every clipped h, and k_finish_outputs sums the SVF from it in
+      // the same order.
       double svf = SV(14);
-      if (D.svf_type == 0) svf += (1.0 - s);
-      else if (D.svf_type == 1) svf += (1.0 - (s * s));
-      else svf += (1.0 - (s * s * s));
+      if (D.refine != 1) {
+        double s = 0.0;
+        if (h > 0.0) s = (j > 0 && j < kSinTable) ? __ldg(&D.sin_lattice[j]) : sin(h);
+        svf = svf + svf_term(s, D.svf_type);
+      }
       a++;
       if (a == D.L) {
-        D.skyview[cell] = svf;  // divided by L in k_finish_outputs
+        if (D.refine != 1) D.skyview[cell] = svf;  // divided by L in k_finish_outputs
         if (D.done) {
           // Completion time of the domain's last cell (batch latency).
           const unsigned long long fin_cells = atomicAdd(&D.done[0], 1ull) + 1ull;
@@ -593,7 +603,7 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
     const int16_t* start_m = doms[dom].start_m;
     if (start_m && (a == 0 || doms[dom].start_all)) {
       m = start_m[(long long)a * doms[dom].ncell + cell];
-      SV(12) = (double)m * (2.0 * doms[dom].hori_acc);
+      SV(12) = (double)m * doms[dom].two_ha;
     }
     const double2 cs = __ldg(&doms[dom].azim_cs[a]);
     SV(9) = cs.x * SV(3) + cs.y * SV(6);
@@ -615,7 +625,7 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
   if (m >= kElevMin && m < kElevMin + kElevTable) {
     ecs = __ldg(&D.elev_cs[m - kElevMin]);
   } else {
-    const double e = (double)m * (2.0 * D.hori_acc);
+    const double e = (double)m * D.two_ha;
     ecs = make_double2(cos(e), sin(e));
   }
   dir.x = (float)(ecs.x * SV(9) + ecs.y * SV(0));
@@ -885,12 +895,26 @@ __global__ void k_finish_outputs(const DomainDesc* __restrict__ doms, int ndom,
   const long long g = order[k];
   const DomainDesc& D = doms[domain_of(doms, ndom, g)];
   const int cell = (int)(g - D.cell_offset);
+  const bool svf_here = D.refine == 1;
+  const double inv_ha = 1.0 / D.hori_acc;
+  double svf = 0.0;
   for (int j = 0; j < D.nhori; j++) {
     double* h = D.horizon + (long long)j * D.ncell + cell;
-    const double deg = (*h / kPi) * 180.0;
+    const double v = *h;
+    if (svf_here) {
+      // v is the clipped h of azimuth j; h > 0 lies on the lattice j_lat *
+      // hori_acc up to the rounding of the elevation sum, which recovers j_lat.
+      double s = 0.0;
+      if (v > 0.0) {
+        const int jl = (int)rint(v * inv_ha);
+        s = (jl > 0 && jl < kSinTable) ? __ldg(&D.sin_lattice[jl]) : sin(v);
+      }
+      svf = svf + svf_term(s, D.svf_type);
+    }
+    const double deg = (v / kPi) * 180.0;
     *h = D.refine == 1 ? deg : deg / (double)D.refine;
   }
-  D.skyview[cell] = D.skyview[cell] / (double)D.L;
+  D.skyview[cell] = (svf_here ? svf : D.skyview[cell]) / (double)D.L;
 }
 
 // Morton keys (2 x 16 bits) of the traced cells' horizontal ENU position.
