@@ -96,7 +96,9 @@ def tune(inputs, args, sample_cells: int = 250_000, reps: int = 2, rounds: int =
     n = min(sample_cells, ncell)
     begin = (ncell - n) // 2
     cells = (begin, begin + n)
-    cur = dict(DEFAULTS)
+    # Start from the first value of each knob in the grid (the library
+    # defaults head the built-in grid).
+    cur = {k: (grid[k][0] if k in grid else v) for k, v in DEFAULTS.items()}
     _time(inputs, args, cells, cur, 1, stream)  # warm-up (allocations, first launch)
     best_ms = _time(inputs, args, cells, cur, reps, stream)
     trials = 1
