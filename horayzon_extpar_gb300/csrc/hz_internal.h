@@ -125,8 +125,14 @@ cudaError_t cell_order(const double* cell_enu, int begin, int count, int id_offs
 // One domain of the persistent search (device-resident array).
 struct DomainDesc {
   const double* cell_enu;     // [3 * ncell] FP64 ENU of cell centres
-  double* cell_frame;         // [9][ncell] sphere normal, north, east (k_cell_frames)
-  float* cell_origin;         // [6][ncell] FP32 ray origin, precise mode: + residual
+  // Per traced cell, indexed by its position p = k - k_begin in `order`
+  // (k_cell_frames): [9][ncell] sphere normal, north, east; [6][ncell] FP32
+  // ray origin and, in precise mode, its residual; optionally [L][3][ncell]
+  // the horizontal direction of every azimuth (null: computed in the search).
+  double* cell_frame;
+  float* cell_origin;
+  double* cell_haz;
+  long long k_begin;          // position in `order` of this domain's first work id
   const Node* nodes;
   const Node4* nodes4;        // BVH4 collapse of nodes (wide traversal only)
   const Tri* tris;

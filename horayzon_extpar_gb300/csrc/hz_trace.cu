@@ -502,6 +502,7 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
 #define SV(k_) st.d(k_)
 #define SO(k_) st.f(k_)
   int dom = st.i(0), cell = st.i(1), a = st.i(2), phase = st.i(3), up = st.i(4), m = st.i(5);
+  int p = st.i(6);
   bool alive = true;
   bool emit = false;
   while (!emit) {
@@ -516,12 +517,13 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       const DomainDesc& D = doms[dom];
       cell = (int)(g - D.cell_offset);
       // Cell frame (mo_lradtopo_horayzon.cpp:694-720) from k_cell_frames.
+      p = (int)(k - D.k_begin);
       const long long nc = D.ncell;
-      const double* fr = D.cell_frame + cell;
+      const double* fr = D.cell_frame + p;
       SV(0) = fr[0]; SV(1) = fr[nc]; SV(2) = fr[2 * nc];
       SV(3) = fr[3 * nc]; SV(4) = fr[4 * nc]; SV(5) = fr[5 * nc];
       SV(6) = fr[6 * nc]; SV(7) = fr[7 * nc]; SV(8) = fr[8 * nc];
-      const float* org = D.cell_origin + cell;
+      const float* org = D.cell_origin + p;
       SO(0) = org[0];
       SO(1) = org[nc];
       SO(2) = org[2 * nc];
@@ -605,10 +607,19 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       m = start_m[(long long)a * doms[dom].ncell + cell];
       SV(12) = (double)m * doms[dom].two_ha;
     }
-    const double2 cs = __ldg(&doms[dom].azim_cs[a]);
-    SV(9) = cs.x * SV(3) + cs.y * SV(6);
-    SV(10) = cs.x * SV(4) + cs.y * SV(7);
-    SV(11) = cs.x * SV(5) + cs.y * SV(8);
+    const double* haz = doms[dom].cell_haz;
+    if (haz) {
+      const long long nc = doms[dom].ncell;
+      haz += (3LL * a) * nc + p;
+      SV(9) = haz[0];
+      SV(10) = haz[nc];
+      SV(11) = haz[2 * nc];
+    } else {
+      const double2 cs = __ldg(&doms[dom].azim_cs[a]);
+      SV(9) = cs.x * SV(3) + cs.y * SV(6);
+      SV(10) = cs.x * SV(4) + cs.y * SV(7);
+      SV(11) = cs.x * SV(5) + cs.y * SV(8);
+    }
     emit = true;
   }
   st.i(3) = phase;
@@ -619,6 +630,7 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
   st.i(2) = a;
   st.i(4) = up;
   st.i(5) = m;
+  st.i(6) = p;
   // Direction at lattice elevation m: cos(e_m) h_a + sin(e_m) U.
   const DomainDesc& D = doms[dom];
   double2 ecs;
@@ -656,10 +668,11 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   // Per-lane search state. FP64: 0-2 sphere normal U, 3-5 north N, 6-8 east
   // E, 9-11 horizontal direction of the current azimuth, 12 elevation
   // accumulator, 13 sector sum, 14 SVF sum. Integers: domain, cell, azimuth,
-  // phase, upward steps, lattice index m of the current elevation. FP32 ray
-  // origin (hi, and lo in precise mode).
+  // phase, upward steps, lattice index m of the current elevation, position
+  // of the cell in the work order. FP32 ray origin (hi, and lo in precise
+  // mode).
   __shared__ double sv[15][kFlatBlock];
-  __shared__ int si[6][kFlatBlock];
+  __shared__ int si[7][kFlatBlock];
   __shared__ float so[6][kFlatBlock];
   __shared__ int wq[2][kFlatBlock / 32];  // per warp: next and end of its chunk of work ids
   constexpr unsigned kFull = 0xffffffffu;
@@ -670,7 +683,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   }
   __syncwarp();
 #pragma unroll
-  for (int q = 0; q < 6; q++) si[q][t] = 0;
+  for (int q = 0; q < 7; q++) si[q][t] = 0;
   si[3][t] = kPhaseStart;
 
   bool alive = true, need = true, last_hit = false;
@@ -848,7 +861,9 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
 }
 
 // Frame and FP32 ray origin of every traced cell, mo_lradtopo_horayzon.cpp:
-// 694-720 (the per-cell kernel's expressions), as [9][ncell] / [6][ncell].
+// 694-720 (the per-cell kernel's expressions), and optionally the horizontal
+// direction cos(theta_a) N + sin(theta_a) E of every azimuth, stored by the
+// cell's position in the work order (the search reads them coalesced).
 template <bool kPrecise>
 __global__ void k_cell_frames(const DomainDesc* __restrict__ doms, int ndom,
                               const int* __restrict__ order, int total) {
@@ -857,6 +872,7 @@ __global__ void k_cell_frames(const DomainDesc* __restrict__ doms, int ndom,
   const long long g = order[k];
   const DomainDesc& D = doms[domain_of(doms, ndom, g)];
   const int cell = (int)(g - D.cell_offset);
+  const long long p = k - D.k_begin;
   const V3 q{D.cell_enu[3LL * cell], D.cell_enu[3LL * cell + 1], D.cell_enu[3LL * cell + 2]};
   V3 normal{q.x - D.centre.x, q.y - D.centre.y, q.z - D.centre.z};
   unit3(normal);
@@ -869,11 +885,11 @@ __global__ void k_cell_frames(const DomainDesc* __restrict__ doms, int ndom,
   const double o64y = q.y + normal.y * D.ray_org_elev;
   const double o64z = q.z + normal.z * D.ray_org_elev;
   const long long nc = D.ncell;
-  double* fr = D.cell_frame + cell;
+  double* fr = D.cell_frame + p;
   fr[0] = normal.x; fr[nc] = normal.y; fr[2 * nc] = normal.z;
   fr[3 * nc] = north.x; fr[4 * nc] = north.y; fr[5 * nc] = north.z;
   fr[6 * nc] = east.x; fr[7 * nc] = east.y; fr[8 * nc] = east.z;
-  float* org = D.cell_origin + cell;
+  float* org = D.cell_origin + p;
   const float ox = (float)o64x, oy = (float)o64y, oz = (float)o64z;
   org[0] = ox;
   org[nc] = oy;
@@ -882,6 +898,15 @@ __global__ void k_cell_frames(const DomainDesc* __restrict__ doms, int ndom,
     org[3 * nc] = (float)(o64x - (double)ox);
     org[4 * nc] = (float)(o64y - (double)oy);
     org[5 * nc] = (float)(o64z - (double)oz);
+  }
+  if (D.cell_haz) {
+    double* hz = D.cell_haz + p;
+    for (int a = 0; a < D.L; a++) {
+      const double2 cs = __ldg(&D.azim_cs[a]);
+      hz[(3LL * a) * nc] = cs.x * north.x + cs.y * east.x;
+      hz[(3LL * a + 1) * nc] = cs.x * north.y + cs.y * east.y;
+      hz[(3LL * a + 2) * nc] = cs.x * north.z + cs.y * east.z;
+    }
   }
 }
 
