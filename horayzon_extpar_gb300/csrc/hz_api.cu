@@ -109,7 +109,6 @@ struct Buffers {
   double* cell_enu;
   double* cell_frame;  // [9][ncell] (persistent search)
   float* cell_origin;  // [6][ncell]
-  double* cell_haz;    // [L][3][ncell] or null (over the memory budget)
   // BVH
   Node* nodes;
   Node4* nodes4;     // wide traversal only
@@ -122,11 +121,6 @@ struct Buffers {
   double* sin_lattice;
   int* err;
 };
-
-// Largest per-domain table of per-azimuth horizontal directions (24 bytes
-// per cell and azimuth) kept for the search; larger domains compute them in
-// the search.
-constexpr long long kHazBudget = 8ll << 30;
 
 // Traversal loop of the persistent search selected by hz_options.kernel.
 int trace_variant(const hz_options& opt) {
@@ -167,10 +161,6 @@ Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhor
   b.cell_enu = c.take<double>(3 * ncell);
   b.cell_frame = c.take<double>(9 * ncell);
   b.cell_origin = c.take<float>(6 * ncell);
-  // Per-azimuth horizontal directions: 24 bytes per cell and azimuth, when
-  // that stays within kHazBudget bytes for the domain.
-  if (L > 0 && 24.0 * (double)L * (double)ncell <= (double)kHazBudget)
-    b.cell_haz = c.take<double>(3 * L * ncell);
   const long long nt = max_tri > 0 ? max_tri : 1;
   b.nodes = c.take<Node>(nt > 1 ? nt - 1 : 1);
   if (wide) b.nodes4 = c.take<Node4>(nt > 1 ? nt - 1 : 1);
@@ -595,7 +585,6 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.cell_enu = b[d].cell_enu;
       D.cell_frame = b[d].cell_frame;
       D.cell_origin = b[d].cell_origin;
-      D.cell_haz = b[d].cell_haz;
       D.k_begin = total;
       D.nodes = b[d].nodes;
       D.nodes4 = b[d].nodes4;

@@ -148,17 +148,17 @@ __global__ void k_gather(const float* __restrict__ vert, const int* __restrict__
   const float3 b = load_vert(vert, i1);
   const float3 c = load_vert(vert, i2);
   Tri r;
-  r.v0 = make_float4(a.x, a.y, a.z, __int_as_float(t));
-  r.v1 = make_float4(b.x, b.y, b.z, 0.f);
-  r.v2 = make_float4(c.x, c.y, c.z, 0.f);
+  r.x = make_float4(a.x, b.x, c.x, __int_as_float(t));
+  r.y = make_float4(a.y, b.y, c.y, 0.f);
+  r.z = make_float4(a.z, b.z, c.z, 0.f);
   tris[s] = r;
-  if (tri_lo) {
+  if (tri_lo) {  // the residuals in the same per-axis layout
     const float3 la = load_vert(vert_lo, i0);
     const float3 lb = load_vert(vert_lo, i1);
     const float3 lc = load_vert(vert_lo, i2);
-    tri_lo[3LL * s + 0] = make_float4(la.x, la.y, la.z, 0.f);
-    tri_lo[3LL * s + 1] = make_float4(lb.x, lb.y, lb.z, 0.f);
-    tri_lo[3LL * s + 2] = make_float4(lc.x, lc.y, lc.z, 0.f);
+    tri_lo[3LL * s + 0] = make_float4(la.x, lb.x, lc.x, 0.f);
+    tri_lo[3LL * s + 1] = make_float4(la.y, lb.y, lc.y, 0.f);
+    tri_lo[3LL * s + 2] = make_float4(la.z, lb.z, lc.z, 0.f);
   }
 }
 
@@ -171,13 +171,12 @@ __device__ __forceinline__ Box leaf_box(const Tri* __restrict__ tris, int ref, f
   Box b = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
   for (int k = s; k < s + c; k++) {
     const Tri t = tris[k];
-    const float4 v[3] = {t.v0, t.v1, t.v2};
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-      b.lx = fminf(b.lx, v[q].x); b.hx = fmaxf(b.hx, v[q].x);
-      b.ly = fminf(b.ly, v[q].y); b.hy = fmaxf(b.hy, v[q].y);
-      b.lz = fminf(b.lz, v[q].z); b.hz = fmaxf(b.hz, v[q].z);
-    }
+    b.lx = fminf(fminf(b.lx, t.x.x), fminf(t.x.y, t.x.z));
+    b.hx = fmaxf(fmaxf(b.hx, t.x.x), fmaxf(t.x.y, t.x.z));
+    b.ly = fminf(fminf(b.ly, t.y.x), fminf(t.y.y, t.y.z));
+    b.hy = fmaxf(fmaxf(b.hy, t.y.x), fmaxf(t.y.y, t.y.z));
+    b.lz = fminf(fminf(b.lz, t.z.x), fminf(t.z.y, t.z.z));
+    b.hz = fmaxf(fmaxf(b.hz, t.z.x), fmaxf(t.z.y, t.z.z));
   }
   b.lx = __fsub_rn(b.lx, pad); b.ly = __fsub_rn(b.ly, pad); b.lz = __fsub_rn(b.lz, pad);
   b.hx = __fadd_rn(b.hx, pad); b.hy = __fadd_rn(b.hy, pad); b.hz = __fadd_rn(b.hz, pad);

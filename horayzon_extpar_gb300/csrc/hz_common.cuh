@@ -57,9 +57,11 @@ struct __align__(16) Node4 {
 };
 constexpr int kStackDepth4 = 96;  // 3 pushes per BVH4 level
 
-// Triangle record, 48 bytes: v0.xyz + original id, v1.xyz, v2.xyz.
+// Triangle record, 48 bytes, one float4 per axis: x = (v0.x, v1.x, v2.x,
+// original id), y = (v0.y, v1.y, v2.y, 0), z = (v0.z, v1.z, v2.z, 0). A ray
+// loads the axes in its own (kx, ky, kz) order by address offset.
 struct __align__(16) Tri {
-  float4 v0, v1, v2;
+  float4 x, y, z;
 };
 
 // Global ENU frame of the domain (mo_lradtopo_horayzon.cpp:611-644).

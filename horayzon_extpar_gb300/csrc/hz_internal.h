@@ -127,11 +127,9 @@ struct DomainDesc {
   const double* cell_enu;     // [3 * ncell] FP64 ENU of cell centres
   // Per traced cell, indexed by its position p = k - k_begin in `order`
   // (k_cell_frames): [9][ncell] sphere normal, north, east; [6][ncell] FP32
-  // ray origin and, in precise mode, its residual; optionally [L][3][ncell]
-  // the horizontal direction of every azimuth (null: computed in the search).
+  // ray origin and, in precise mode, its residual.
   double* cell_frame;
   float* cell_origin;
-  double* cell_haz;
   long long k_begin;          // position in `order` of this domain's first work id
   const Node* nodes;
   const Node4* nodes4;        // BVH4 collapse of nodes (wide traversal only)

@@ -109,40 +109,40 @@ __device__ __forceinline__ bool tri_hit_rel(const Ray& r, float Akx, float Aky, 
 }
 
 // Reference arithmetic: FP32 vertices minus the FP32 origin in the domain's
-// global ENU frame (mo_lradtopo_horayzon.cpp:403-410, 715-720).
-__device__ __forceinline__ bool tri_hit(const Ray& r, const float4 v0, const float4 v1,
-                                        const float4 v2) {
-  return tri_hit_rel(r, __fsub_rn(sel3(v0.x, v0.y, v0.z, r.kx), r.pox),
-                     __fsub_rn(sel3(v0.x, v0.y, v0.z, r.ky), r.poy),
-                     __fsub_rn(sel3(v0.x, v0.y, v0.z, r.kz), r.poz),
-                     __fsub_rn(sel3(v1.x, v1.y, v1.z, r.kx), r.pox),
-                     __fsub_rn(sel3(v1.x, v1.y, v1.z, r.ky), r.poy),
-                     __fsub_rn(sel3(v1.x, v1.y, v1.z, r.kz), r.poz),
-                     __fsub_rn(sel3(v2.x, v2.y, v2.z, r.kx), r.pox),
-                     __fsub_rn(sel3(v2.x, v2.y, v2.z, r.ky), r.poy),
-                     __fsub_rn(sel3(v2.x, v2.y, v2.z, r.kz), r.poz));
+// global ENU frame (mo_lradtopo_horayzon.cpp:403-410, 715-720). X, Y, Z are
+// the triangle's (kx, ky, kz) axes: (v0, v1, v2) components of each.
+__device__ __forceinline__ bool tri_hit(const Ray& r, const float4 X, const float4 Y,
+                                        const float4 Z) {
+  return tri_hit_rel(r, __fsub_rn(X.x, r.pox), __fsub_rn(Y.x, r.poy), __fsub_rn(Z.x, r.poz),
+                     __fsub_rn(X.y, r.pox), __fsub_rn(Y.y, r.poy), __fsub_rn(Z.y, r.poz),
+                     __fsub_rn(X.z, r.pox), __fsub_rn(Y.z, r.poy), __fsub_rn(Z.z, r.poz));
 }
 
 // Precise arithmetic: vertices and origin as FP32 hi + lo pairs (~48-bit
 // FP64 values); the origin-relative vector (hi - o_hi) + (lo - o_lo) is
 // accurate to FP32 relative to its own length, i.e. centimetres become
-// micrometres for the triangles next to the cell.
+// micrometres for the triangles next to the cell. LX, LY, LZ: the residuals.
 __device__ __forceinline__ float rel(float vh, float vl, float oh, float ol) {
   return __fadd_rn(__fsub_rn(vh, oh), __fsub_rn(vl, ol));
 }
-__device__ __forceinline__ bool tri_hit_hl(const Ray& r, const float4 v0, const float4 v1,
-                                           const float4 v2, const float4 l0, const float4 l1,
-                                           const float4 l2) {
-  return tri_hit_rel(
-      r, rel(sel3(v0.x, v0.y, v0.z, r.kx), sel3(l0.x, l0.y, l0.z, r.kx), r.pox, r.plx),
-      rel(sel3(v0.x, v0.y, v0.z, r.ky), sel3(l0.x, l0.y, l0.z, r.ky), r.poy, r.ply),
-      rel(sel3(v0.x, v0.y, v0.z, r.kz), sel3(l0.x, l0.y, l0.z, r.kz), r.poz, r.plz),
-      rel(sel3(v1.x, v1.y, v1.z, r.kx), sel3(l1.x, l1.y, l1.z, r.kx), r.pox, r.plx),
-      rel(sel3(v1.x, v1.y, v1.z, r.ky), sel3(l1.x, l1.y, l1.z, r.ky), r.poy, r.ply),
-      rel(sel3(v1.x, v1.y, v1.z, r.kz), sel3(l1.x, l1.y, l1.z, r.kz), r.poz, r.plz),
-      rel(sel3(v2.x, v2.y, v2.z, r.kx), sel3(l2.x, l2.y, l2.z, r.kx), r.pox, r.plx),
-      rel(sel3(v2.x, v2.y, v2.z, r.ky), sel3(l2.x, l2.y, l2.z, r.ky), r.poy, r.ply),
-      rel(sel3(v2.x, v2.y, v2.z, r.kz), sel3(l2.x, l2.y, l2.z, r.kz), r.poz, r.plz));
+__device__ __forceinline__ bool tri_hit_hl(const Ray& r, const float4 X, const float4 Y,
+                                           const float4 Z, const float4 LX, const float4 LY,
+                                           const float4 LZ) {
+  return tri_hit_rel(r, rel(X.x, LX.x, r.pox, r.plx), rel(Y.x, LY.x, r.poy, r.ply),
+                     rel(Z.x, LZ.x, r.poz, r.plz), rel(X.y, LX.y, r.pox, r.plx),
+                     rel(Y.y, LY.y, r.poy, r.ply), rel(Z.y, LZ.y, r.poz, r.plz),
+                     rel(X.z, LX.z, r.pox, r.plx), rel(Y.z, LY.z, r.poy, r.ply),
+                     rel(Z.z, LZ.z, r.poz, r.plz));
+}
+
+// Triangle k's axes in the ray's (kx, ky, kz) order (Tri: one float4 per
+// axis), and the same for the precise residuals.
+__device__ __forceinline__ void load_tri(const Tri* __restrict__ tris, const Ray& r, int k,
+                                         float4& X, float4& Y, float4& Z) {
+  const float4* t = reinterpret_cast<const float4*>(tris + k);
+  X = __ldg(t + r.kx);
+  Y = __ldg(t + r.ky);
+  Z = __ldg(t + r.kz);
 }
 
 // Conservative slab test: the boxes carry a margin far above the rounding of
@@ -184,10 +184,9 @@ __device__ bool occluded(const Ray& r, const Node* __restrict__ nodes,
       const int s = leaf_start(ref), c = leaf_count(ref);
       for (int k = s; k < s + c; k++) {
         if (kCount) ntest++;
-        const float4 v0 = __ldg(&tris[k].v0);
-        const float4 v1 = __ldg(&tris[k].v1);
-        const float4 v2 = __ldg(&tris[k].v2);
-        if (tri_hit(r, v0, v1, v2)) return true;
+        float4 X, Y, Z;
+        load_tri(tris, r, k, X, Y, Z);
+        if (tri_hit(r, X, Y, Z)) return true;
       }
     } else {
       if (kCount) nvis++;
@@ -453,16 +452,13 @@ __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, co
 template <bool kPrecise>
 __device__ __forceinline__ bool test_tri(const Tri* __restrict__ tris,
                                          const float4* __restrict__ tri_lo, const Ray& r, int k) {
-  const float4 v0 = __ldg(&tris[k].v0);
-  const float4 v1 = __ldg(&tris[k].v1);
-  const float4 v2 = __ldg(&tris[k].v2);
+  float4 X, Y, Z;
+  load_tri(tris, r, k, X, Y, Z);
   if (kPrecise) {
-    const float4 l0 = __ldg(&tri_lo[3LL * k]);
-    const float4 l1 = __ldg(&tri_lo[3LL * k + 1]);
-    const float4 l2 = __ldg(&tri_lo[3LL * k + 2]);
-    return tri_hit_hl(r, v0, v1, v2, l0, l1, l2);
+    const float4* l = tri_lo + 3LL * k;
+    return tri_hit_hl(r, X, Y, Z, __ldg(l + r.kx), __ldg(l + r.ky), __ldg(l + r.kz));
   }
-  return tri_hit(r, v0, v1, v2);
+  return tri_hit(r, X, Y, Z);
 }
 
 // One azimuth's SVF term for sin(h) = s (cpp:333-358).
@@ -607,19 +603,10 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       m = start_m[(long long)a * doms[dom].ncell + cell];
       SV(12) = (double)m * doms[dom].two_ha;
     }
-    const double* haz = doms[dom].cell_haz;
-    if (haz) {
-      const long long nc = doms[dom].ncell;
-      haz += (3LL * a) * nc + p;
-      SV(9) = haz[0];
-      SV(10) = haz[nc];
-      SV(11) = haz[2 * nc];
-    } else {
-      const double2 cs = __ldg(&doms[dom].azim_cs[a]);
-      SV(9) = cs.x * SV(3) + cs.y * SV(6);
-      SV(10) = cs.x * SV(4) + cs.y * SV(7);
-      SV(11) = cs.x * SV(5) + cs.y * SV(8);
-    }
+    const double2 cs = __ldg(&doms[dom].azim_cs[a]);
+    SV(9) = cs.x * SV(3) + cs.y * SV(6);
+    SV(10) = cs.x * SV(4) + cs.y * SV(7);
+    SV(11) = cs.x * SV(5) + cs.y * SV(8);
     emit = true;
   }
   st.i(3) = phase;
@@ -861,9 +848,8 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
 }
 
 // Frame and FP32 ray origin of every traced cell, mo_lradtopo_horayzon.cpp:
-// 694-720 (the per-cell kernel's expressions), and optionally the horizontal
-// direction cos(theta_a) N + sin(theta_a) E of every azimuth, stored by the
-// cell's position in the work order (the search reads them coalesced).
+// 694-720 (the per-cell kernel's expressions), stored by the cell's position
+// in the work order (the search reads them coalesced).
 template <bool kPrecise>
 __global__ void k_cell_frames(const DomainDesc* __restrict__ doms, int ndom,
                               const int* __restrict__ order, int total) {
@@ -898,15 +884,6 @@ __global__ void k_cell_frames(const DomainDesc* __restrict__ doms, int ndom,
     org[3 * nc] = (float)(o64x - (double)ox);
     org[4 * nc] = (float)(o64y - (double)oy);
     org[5 * nc] = (float)(o64z - (double)oz);
-  }
-  if (D.cell_haz) {
-    double* hz = D.cell_haz + p;
-    for (int a = 0; a < D.L; a++) {
-      const double2 cs = __ldg(&D.azim_cs[a]);
-      hz[(3LL * a) * nc] = cs.x * north.x + cs.y * east.x;
-      hz[(3LL * a + 1) * nc] = cs.x * north.y + cs.y * east.y;
-      hz[(3LL * a + 2) * nc] = cs.x * north.z + cs.y * east.z;
-    }
   }
 }
 
