@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(128) k_trace_exact(TraceParams p) {
 // ---------------------------------------------------------------------------
 constexpr int kFlatBlock = 128;
 #ifndef HZ_WARP_MIN_BLOCKS
-#define HZ_WARP_MIN_BLOCKS 6  // resident blocks per SM the register budget targets
+#define HZ_WARP_MIN_BLOCKS 8  // resident blocks per SM the register budget targets
 #endif
 
 #ifndef HZ_NODE_STEPS
@@ -735,7 +735,12 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
           first = wq[0][w];
           wq[0][w] += take;
           if (take < nreq) {
-            const int grab = max(chunk, nreq - take);
+            // Near the end of the queue (less than one chunk per warp of the
+            // launch left) a warp takes only what it needs, so the last
+            // cells spread over more warps.
+            const int left = total - *(volatile int*)work;
+            const bool tail = left < (int)min(2147483647ll, (long long)gridDim.x * (kFlatBlock / 32) * chunk);
+            const int grab = tail ? nreq - take : max(chunk, nreq - take);
             nb = atomicAdd(work, grab);
             wq[0][w] = nb + (nreq - take);
             wq[1][w] = nb + grab;
