@@ -586,6 +586,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.cell_frame = b[d].cell_frame;
       D.cell_origin = b[d].cell_origin;
       D.k_begin = total;
+      D.cell_begin = P.cell_begin;
       D.nodes = b[d].nodes;
       D.nodes4 = b[d].nodes4;
       D.tris = b[d].tris;

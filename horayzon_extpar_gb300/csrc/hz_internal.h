@@ -131,6 +131,7 @@ struct DomainDesc {
   double* cell_frame;
   float* cell_origin;
   long long k_begin;          // position in `order` of this domain's first work id
+  int cell_begin;             // first traced cell (cells cell_begin .. + ncell_traced)
   const Node* nodes;
   const Node4* nodes4;        // BVH4 collapse of nodes (wide traversal only)
   const Tri* tris;

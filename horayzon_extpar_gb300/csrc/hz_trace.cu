@@ -895,13 +895,20 @@ __global__ void k_cell_frames(const DomainDesc* __restrict__ doms, int ndom,
 // The search's sums to outputs (cpp:736-754): horizon sector sums [rad] ->
 // degrees and mean over refine_factor; SVF sum -> mean over the azimuths.
 // x / 1.0 == x exactly, so that division is skipped for refine_factor 1.
-__global__ void k_finish_outputs(const DomainDesc* __restrict__ doms, int ndom,
-                                 const int* __restrict__ order, int total) {
+// One thread per traced cell in index order (coalesced rows of horizon):
+// thread k is the (k - k_begin)-th traced cell of the domain holding
+// position k.
+__global__ void k_finish_outputs(const DomainDesc* __restrict__ doms, int ndom, int total) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= total) return;
-  const long long g = order[k];
-  const DomainDesc& D = doms[domain_of(doms, ndom, g)];
-  const int cell = (int)(g - D.cell_offset);
+  int lo = 0, hi = ndom - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (doms[mid].k_begin <= k) lo = mid;
+    else hi = mid - 1;
+  }
+  const DomainDesc& D = doms[lo];
+  const int cell = D.cell_begin + (int)(k - D.k_begin);
   const bool svf_here = D.refine == 1;
   const double inv_ha = 1.0 / D.hori_acc;
   double svf = 0.0;
@@ -1077,7 +1084,7 @@ cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, i
   cudaError_t e =
       launch_search(doms, ndom, order, total, work, counters, err, k, count_work, precise, s);
   if (e != cudaSuccess) return e;
-  k_finish_outputs<<<grid_for(total, 256), 256, 0, s>>>(doms, ndom, order, total);
+  k_finish_outputs<<<grid_for(total, 256), 256, 0, s>>>(doms, ndom, total);
   note_launches(1);
   return cudaGetLastError();
 }
