@@ -20,6 +20,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/horayzon_gb300.h"
 #include "hz_internal.h"
 
@@ -39,6 +41,20 @@ void log_line(const char* fmt, ...) {
   va_end(ap);
   g_log += buf;
 }
+// NVTX range of the current phase of a call (host side, as enqueued), for
+// profilers that show NVTX; a no-op without one attached.
+struct PhaseRange {
+  bool open = false;
+  void next(const char* name) {
+    if (open) nvtxRangePop();
+    nvtxRangePushA(name);
+    open = true;
+  }
+  ~PhaseRange() {
+    if (open) nvtxRangePop();
+  }
+};
+
 const char* kRule =
     "-------------------------------------------------------------------------------\n";
 
@@ -251,6 +267,11 @@ struct Engine {
 
   int reserve(size_t bytes, cudaStream_t s) {
     if (bytes <= cap) return HZ_OK;
+    // Failure injection for tests of the error path (no GPU fault involved):
+    // HZ_INJECT_ALLOC_FAILURE=1 makes every growth of the workspace fail.
+    const char* inject = getenv("HZ_INJECT_ALLOC_FAILURE");
+    if (inject && inject[0] == '1')
+      return fail(HZ_ERR_CUDA, "cudaMalloc of %zu bytes failed: injected failure", bytes);
     HZ_CUDA(cudaStreamSynchronize(s));
     if (arena) HZ_CUDA(cudaFree(arena));
     arena = nullptr;
@@ -394,6 +415,8 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   HZ_CUDA(cudaMemsetAsync(bb.counters + 12, 0xFF, 2 * sizeof(unsigned long long), s));
 #endif
   HZ_CUDA(cudaMemsetAsync(bb.done, 0, 2 * sizeof(unsigned long long) * (size_t)n, s));
+  PhaseRange phase;
+  phase.next("hz: mesh");
   HZ_CUDA(cudaEventRecord(E.ev[0], s));
 
   // ---- mesh (cpp:228-317) ----
@@ -454,6 +477,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
                      b[d].cell_enu, b[d].vert_lo, s));
   }
   HZ_CUDA(cudaEventRecord(E.ev[1], s));
+  phase.next("hz: bvh");
   if (stop == Stop::kEnu) return HZ_OK;
 
   // ---- BVH (cpp:395-432) ----
@@ -461,6 +485,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     HZ_CUDA(bvh_build(b[d].vert32, b[d].vot, out->n_tri[d], b[d].nodes, b[d].tris, b[d].bvh, s,
                       b[d].vert_lo, b[d].tri_lo, b[d].nodes4, opt.leaf_size));
   HZ_CUDA(cudaEventRecord(E.ev[2], s));
+  phase.next("hz: search");
 
   // ---- horizon + SVF (cpp:651-761) ----
   const double hori_acc = deg2rad(0.25);
@@ -634,6 +659,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
                        opt.count_work != 0, b[0].tri_lo != nullptr, s));
   }
   HZ_CUDA(cudaEventRecord(E.ev[3], s));
+  phase.next("hz: readback");
 
   // Counters, error word, and per-domain completion times.
   unsigned long long* rb = pin;  // words 0..15 (descriptors live beyond word 64)

@@ -25,7 +25,24 @@ from .horizon_svf import horizon_svf_comp_device
 
 N_IN = 32
 N_HID = 64
+N_PARAMS = N_IN * N_HID + N_HID + N_HID * N_HID + N_HID + N_HID + 1  # 6337
 TARGET_MIN_J = -16  # -4 deg in quarter degrees
+
+
+def save_params(path: str, params) -> None:
+    """Writes trained parameters (FP32, packed as hz_mlp_train_step uses them;
+    the kernels round the weights to BF16 when they load them)."""
+    p = np.ascontiguousarray(params, dtype=np.float32).ravel()
+    if p.size != N_PARAMS:
+        raise ValueError("expected %d parameters, got %d" % (N_PARAMS, p.size))
+    np.save(path, p)
+
+
+def load_params(path: str) -> np.ndarray:
+    p = np.load(path).astype(np.float32).ravel()
+    if p.size != N_PARAMS:
+        raise ValueError("expected %d parameters, got %d" % (N_PARAMS, p.size))
+    return p
 
 
 def num_params() -> int:

@@ -1,5 +1,6 @@
 """The FP64 MLP oracle itself: gradients against finite differences (CPU)."""
 import numpy as np
+import pytest
 
 from oracle import mlp_ref
 
@@ -26,3 +27,13 @@ def test_bf16_rounding():
     assert r[0] == 1.0 and r[1] == 1.0  # tie to even
     assert r[2] == np.float32(1.0078125)
     assert abs(r[3] + 3.140625) < 1e-6 and r[4] == 0.0
+
+
+def test_mlp_params_save_load_round_trip(tmp_path):
+    from horayzon_extpar_gb300 import learned
+    p = np.random.default_rng(0).normal(size=learned.N_PARAMS).astype(np.float32)
+    path = str(tmp_path / "mlp.npy")
+    learned.save_params(path, p)
+    np.testing.assert_array_equal(learned.load_params(path), p)
+    with pytest.raises(ValueError):
+        learned.save_params(path, p[:10])
