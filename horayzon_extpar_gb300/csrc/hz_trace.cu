@@ -367,10 +367,34 @@ constexpr int kFlatBlock = 128;
 
 enum : int { kPhaseStart = 0, kPhaseFirst = 1, kPhaseUp = 2, kPhaseDown = 3 };
 
+#ifndef HZ_STACK_TOP
+#define HZ_STACK_TOP 1  // 1: the top stack entry lives in a register
+#endif
+// Traversal stack: entries in `stack` (local memory) below a top entry held
+// in a register (kEmptyRef when the stack is empty), so that a pop returns at
+// once and the reload of the next top overlaps with the node fetch.
+__device__ __forceinline__ void stk_push(int* stack, int& sp, int& top, int x) {
+#if HZ_STACK_TOP
+  if (top != kEmptyRef) stack[sp++] = top;
+  top = x;
+#else
+  stack[sp++] = x;
+#endif
+}
+__device__ __forceinline__ int stk_pop(int* stack, int& sp, int& top) {
+#if HZ_STACK_TOP
+  const int r = top;
+  top = sp > 0 ? stack[--sp] : kEmptyRef;
+  return r;
+#else
+  return sp > 0 ? stack[--sp] : kEmptyRef;
+#endif
+}
+
 // Visits internal node `ref`: descends into the nearer hit child (pushing the
 // other), or pops. Returns false on stack overflow.
 __device__ __forceinline__ bool visit_node(const Node* __restrict__ nodes, const Ray& r,
-                                           int& ref, int* stack, int& sp) {
+                                           int& ref, int* stack, int& sp, int& top) {
   const Node* nd = nodes + ref;
   const float4 na = __ldg(&nd->a);
   const float4 nb = __ldg(&nd->b);
@@ -381,16 +405,16 @@ __device__ __forceinline__ bool visit_node(const Node* __restrict__ nodes, const
   const bool h0 = box_hit(r, na.x, na.y, na.z, na.w, nc.x, nc.y, t0);
   const bool h1 = c1 != kEmptyRef && box_hit(r, nb.x, nb.y, nb.z, nb.w, nc.z, nc.w, t1);
   if (h0 && h1) {
-    if (sp >= kStackDepth) return false;
+    if (sp >= kStackDepth - 1) return false;
     const bool near0 = t0 <= t1;
-    stack[sp++] = near0 ? c1 : c0;
+    stk_push(stack, sp, top, near0 ? c1 : c0);
     ref = near0 ? c0 : c1;
   } else if (h0) {
     ref = c0;
   } else if (h1) {
     ref = c1;
   } else {
-    ref = sp > 0 ? stack[--sp] : kEmptyRef;
+    ref = stk_pop(stack, sp, top);
   }
   return true;
 }
@@ -399,7 +423,7 @@ __device__ __forceinline__ bool visit_node(const Node* __restrict__ nodes, const
 // other hit children, farthest first; pops when no child is hit. Returns false
 // on stack overflow.
 __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, const Ray& r,
-                                            int& ref, int* stack, int& sp) {
+                                            int& ref, int* stack, int& sp, int& top) {
   // Planes in node order lo.x, hi.x, lo.y, hi.y, lo.z, hi.z: the near plane
   // of an axis is lo + n (n = 1 for a negative inverse direction).
   const float4* pl = reinterpret_cast<const float4*>(nodes4 + ref);
@@ -436,14 +460,14 @@ __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, co
   cx(t1, r1, t2, r2);
 #endif
   if (t0 == INFINITY) {
-    ref = sp > 0 ? stack[--sp] : kEmptyRef;
+    ref = stk_pop(stack, sp, top);
     return true;
   }
   const int extra = (t1 != INFINITY) + (t2 != INFINITY) + (t3 != INFINITY);
-  if (sp + extra > kStackDepth4) return false;
-  if (t3 != INFINITY) stack[sp++] = r3;
-  if (t2 != INFINITY) stack[sp++] = r2;
-  if (t1 != INFINITY) stack[sp++] = r1;
+  if (sp + extra >= kStackDepth4) return false;
+  if (t3 != INFINITY) stk_push(stack, sp, top, r3);
+  if (t2 != INFINITY) stk_push(stack, sp, top, r2);
+  if (t1 != INFINITY) stk_push(stack, sp, top, r1);
   ref = r0;
   return true;
 }
@@ -674,7 +698,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   si[3][t] = kPhaseStart;
 
   bool alive = true, need = true, last_hit = false;
-  int ref = kEmptyRef, sp = 0;
+  int ref = kEmptyRef, sp = 0, top = kEmptyRef;
   // Postponed leaf as next triangle << 4 | triangles left (0 = none).
   int pl0 = 0;
   int stack[kWide ? kStackDepth4 : kStackDepth];
@@ -699,7 +723,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   auto settle = [&]() {
     if (ref < 0 && ref != kEmptyRef && pl0 == 0) {
       pl0 = (leaf_start(ref) << 4) | leaf_count(ref);
-      ref = sp > 0 ? stack[--sp] : kEmptyRef;
+      ref = stk_pop(stack, sp, top);
     }
     if (ref == kEmptyRef && pl0 == 0) {
       need = true;
@@ -773,6 +797,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
           r = make_ray(so[0][t], so[1][t], so[2][t], d.x, d.y, d.z, D.tfar);
         ref = D.root;
         sp = 0;
+        top = kEmptyRef;
         pl0 = 0;
         need = false;
         rays++;
@@ -794,8 +819,8 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     for (int step = 0; step < HZ_NODE_STEPS; step++) {
       if (alive && !need && ref >= 0) {
         if (kCount) nvis++;
-        if (!(kWide ? visit_node4(nodes4, r, ref, stack, sp)
-                    : visit_node(nodes, r, ref, stack, sp))) {
+        if (!(kWide ? visit_node4(nodes4, r, ref, stack, sp, top)
+                    : visit_node(nodes, r, ref, stack, sp, top))) {
           atomicOr(err, kErrStack);
           need = true;
           last_hit = true;
