@@ -235,8 +235,63 @@ BatchBuffers carve_batch(Carver& c, int n, long long total_cells) {
   return b;
 }
 
+// Stream capture of a stretch of a call into a CUDA graph. Inactive: the
+// work is launched directly. An early return inside the stretch ends the
+// capture and drops the partial graph.
+// The capture runs on the engine's own stream (the caller's may be the
+// legacy default stream, which cannot be captured); the graph is launched on
+// the caller's stream.
+struct Capture {
+  cudaStream_t s;       // captured
+  cudaStream_t launch;  // the graph's stream
+  bool active;
+  bool capturing = false;
+  Capture(cudaStream_t st, cudaStream_t call, bool on) : s(st), launch(call), active(on) {}
+  cudaError_t begin() {
+    if (!active) return cudaSuccess;
+    const cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    capturing = e == cudaSuccess;
+    return e;
+  }
+  // A timing event: recorded as a node of the graph while capturing.
+  cudaError_t record(cudaEvent_t ev) {
+    return capturing ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal)
+                     : cudaEventRecord(ev, s);
+  }
+  // Ends the capture, updates the cached executable graph in place (or
+  // instantiates it when the shape changed) and launches it.
+  cudaError_t end_and_launch(cudaGraphExec_t* exec) {
+    if (!capturing) return cudaSuccess;
+    capturing = false;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (e != cudaSuccess) return e;
+    if (*exec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(*exec, g, &info) != cudaSuccess) {
+        (void)cudaGetLastError();
+        cudaGraphExecDestroy(*exec);
+        *exec = nullptr;
+      }
+    }
+    if (!*exec) e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return e;
+    return cudaGraphLaunch(*exec, launch);
+  }
+  ~Capture() {
+    if (capturing) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      (void)cudaGetLastError();
+    }
+  }
+};
+
 struct Engine {
   int device = -1;
+  cudaGraphExec_t graph = nullptr;  // the last captured call (Capture)
   std::mutex mu;
   void* arena = nullptr;
   size_t cap = 0;
@@ -289,6 +344,8 @@ struct Engine {
   }
 
   void release() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
     if (arena) cudaFree(arena);
     arena = nullptr;
     cap = 0;
@@ -473,10 +530,25 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     const double radius = sqrt(so[0] * so[0] + so[1] * so[1] + so[2] * so[2]);
     out->origin_lat[d] = rad2deg(asin(so[2] / radius));
     out->origin_lon[d] = rad2deg(atan2(so[1], so[0]));
+  }
+
+  // From here to the readback the host waits for nothing (except for the
+  // learned start's raster sizing): the work is captured into a CUDA graph,
+  // kept on the engine and updated in place for the next call of the same
+  // shape, and launched as one unit.
+  const bool learned_run = stop == Stop::kFull && b[0].rz != nullptr;
+  cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+  HZ_CUDA(cudaStreamIsCapturing(s, &cap_status));
+  Capture cap(E.stream, s, stop == Stop::kFull && !learned_run && !opt.direct_launch &&
+                     opt.kernel != HZ_KERNEL_PER_CELL &&
+                     cap_status == cudaStreamCaptureStatusNone);
+  HZ_CUDA(cap.begin());
+  const cudaStream_t s_call = s;
+  if (cap.capturing) s = cap.s;
+  for (int d = 0; d < n; d++)
     HZ_CUDA(mesh_enu(b[d].ecef, out->n_mv[d], pr[d].ncell, frames[d], b[d].vert32,
                      b[d].cell_enu, b[d].vert_lo, s));
-  }
-  HZ_CUDA(cudaEventRecord(E.ev[1], s));
+  HZ_CUDA(cap.record(E.ev[1]));
   phase.next("hz: bvh");
   if (stop == Stop::kEnu) return HZ_OK;
 
@@ -484,7 +556,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   for (int d = 0; d < n; d++)
     HZ_CUDA(bvh_build(b[d].vert32, b[d].vot, out->n_tri[d], b[d].nodes, b[d].tris, b[d].bvh, s,
                       b[d].vert_lo, b[d].tri_lo, b[d].nodes4, opt.leaf_size));
-  HZ_CUDA(cudaEventRecord(E.ev[2], s));
+  HZ_CUDA(cap.record(E.ev[2]));
   phase.next("hz: search");
 
   // ---- horizon + SVF (cpp:651-761) ----
@@ -658,7 +730,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     HZ_CUDA(trace_flat(bb.doms, n, bb.order, (int)total, bb.work, bb.counters, bb.err, knobs,
                        opt.count_work != 0, b[0].tri_lo != nullptr, s));
   }
-  HZ_CUDA(cudaEventRecord(E.ev[3], s));
+  HZ_CUDA(cap.record(E.ev[3]));
   phase.next("hz: readback");
 
   // Counters, error word, and per-domain completion times.
@@ -675,6 +747,8 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   HZ_CUDA(cudaMemcpyAsync(rb + 32, bb.counters, kCounterWords * sizeof(unsigned long long),
                           cudaMemcpyDeviceToHost, s));
 #endif
+  HZ_CUDA(cap.end_and_launch(&E.graph));
+  s = s_call;
   HZ_CUDA(cudaStreamSynchronize(s));
 #ifdef HZ_DIAG
   fprintf(stderr, "hz_diag");

@@ -73,7 +73,8 @@ def _check_args(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_t
 
 def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
              advance_min=0, precision=0, mlp_params=None, raw_index=None, features=None,
-             mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0):
+             mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0,
+             direct_launch=False):
     begin, count = (0, 0) if cells is None else (int(cells[0]), int(cells[1]) - int(cells[0]))
     opt = _lib.default_options(device=int(device), count_work=int(bool(count_work)),
                                elev_floor_deg=float(elev_floor_deg),
@@ -81,7 +82,8 @@ def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
                                cell_count=count, kernel=int(kernel),
                                advance_min=int(advance_min), precision=int(precision),
                                leaf_min=int(leaf_min), leaf_size=int(leaf_size),
-                               queue_chunk=int(queue_chunk))
+                               queue_chunk=int(queue_chunk),
+                               direct_launch=int(bool(direct_launch)))
     if mlp_params is not None:
         p = np.ascontiguousarray(mlp_params, dtype=np.float32)
         if p.size != _lib.load().hz_mlp_num_params():
@@ -102,7 +104,8 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
                         *, device=-1, count_work=False, elev_floor_deg=-85.0,
                         verbose=False, return_stats=False, cells=None, kernel=0,
                         advance_min=0, precision=0, mlp_params=None,
-                        mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0):
+                        mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0,
+                        direct_launch=False):
     """Compute the terrain horizon and sky view factor on the GPU.
 
     Arguments and returns as horizon_svf.pyx:15-76: FP64 1-D ``clon, clat``
@@ -113,9 +116,10 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
     range ``cells=(begin, end)`` to trace (entries outside it are NaN), the
     search ``kernel`` (0 persistent, 1 one thread per cell, 2 the
     persistent search on the binary BVH), its ``advance_min`` / ``leaf_min``
-    knobs, the work-queue ``queue_chunk`` and the BVH ``leaf_size`` and, with
-    ``return_stats``, a third
-    return value with ray counts and phase times.
+    knobs, the work-queue ``queue_chunk``, the BVH ``leaf_size``,
+    ``direct_launch`` (launch each kernel directly instead of replaying the
+    captured CUDA graph of the BVH build and search) and, with
+    ``return_stats``, a third return value with ray counts and phase times.
     """
     clon = _typed("clon", clon, np.float64, 1)
     clat = _typed("clat", clat, np.float64, 1)
@@ -142,7 +146,8 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
     L = _lib.load()
     opt = _options(device, count_work, elev_floor_deg, verbose, cells, kernel, advance_min,
                    precision, mlp_params, mlp_every_azimuth=mlp_every_azimuth,
-                   leaf_min=leaf_min, leaf_size=leaf_size, queue_chunk=queue_chunk)
+                   leaf_min=leaf_min, leaf_size=leaf_size, queue_chunk=queue_chunk,
+                   direct_launch=direct_launch)
     st = _lib.Stats()
     rc = L.hz_horizon_svf(clon.ctypes.data_as(_D), clat.ctypes.data_as(_D),
                           hsurf.ctypes.data_as(_D), vlon.ctypes.data_as(_D),
@@ -163,7 +168,7 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
                             count_work=False, elev_floor_deg=-85.0, cells=None, kernel=0,
                             advance_min=0, precision=0, mlp_params=None, raw_index=None,
                             features=None, mlp_every_azimuth=False, leaf_min=0,
-                            leaf_size=0, queue_chunk=0):
+                            leaf_size=0, queue_chunk=0, direct_launch=False):
     """Same computation on CUDA tensors (torch) already resident on one GPU.
 
     Inputs: contiguous float64 / int32 tensors on the same device, layouts as
@@ -200,7 +205,8 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
     L = _lib.load()
     opt = _options(dev.index if dev.index is not None else -1, count_work,
                    elev_floor_deg, False, cells, kernel, advance_min, precision, mlp_params,
-                   raw_index, features, mlp_every_azimuth, leaf_min, leaf_size, queue_chunk)
+                   raw_index, features, mlp_every_azimuth, leaf_min, leaf_size, queue_chunk,
+                   direct_launch)
     st = _lib.Stats()
     rc = L.hz_horizon_svf_device(clon.data_ptr(), clat.data_ptr(), hsurf.data_ptr(),
                                  vlon.data_ptr(), vlat.data_ptr(),
@@ -256,7 +262,7 @@ def mesh_enu32(clon, clat, hsurf, vlon, vlat, cells_of_vertex, grid_type, device
 def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_deg=-85.0,
                            advance_min=0, return_stats=False, precision=0, mlp_params=None,
                            mlp_every_azimuth=False, kernel=0, leaf_min=0, leaf_size=0,
-                           queue_chunk=0):
+                           queue_chunk=0, direct_launch=False):
     """Many independent domains in one call (one persistent search launch).
 
     ``domains``: sequence of ``(inputs, args)`` with ``inputs`` the six arrays
@@ -284,7 +290,8 @@ def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_d
     arr = (_lib.Domain * len(structs))(*structs)
     opt = _options(device, count_work, elev_floor_deg, False, None, kernel, advance_min,
                    precision, mlp_params, mlp_every_azimuth=mlp_every_azimuth,
-                   leaf_min=leaf_min, leaf_size=leaf_size, queue_chunk=queue_chunk)
+                   leaf_min=leaf_min, leaf_size=leaf_size, queue_chunk=queue_chunk,
+                   direct_launch=direct_launch)
     st = _lib.Stats()
     rc = _lib.load().hz_horizon_svf_batch(arr, len(structs), 0, None, C.byref(opt),
                                           C.byref(st))

@@ -75,6 +75,8 @@ typedef struct hz_options {
     int32_t leaf_size;       /* most triangles per BVH leaf (1..8; 0 = 2) */
     int32_t queue_chunk;     /* persistent kernel: consecutive cells (Morton order) a
                                 warp takes from the work queue at a time (0 = 32) */
+    int32_t direct_launch;   /* 1: launch every kernel directly instead of replaying a
+                                captured CUDA graph of the BVH build and search */
 } hz_options;
 
 enum {

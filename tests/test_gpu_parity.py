@@ -280,3 +280,43 @@ def test_gpu_queue_chunk_keeps_results(small_domain, queue_chunk):
     np.testing.assert_array_equal(s0, s1)
     assert st0["num_rays"] == st1["num_rays"]
 
+
+
+def test_gpu_graph_replay_matches_direct_launch(small_domain):
+    """The captured CUDA graph (replayed, updated in place for a call of the
+    same shape, re-instantiated for another shape) gives the same results as
+    launching every kernel directly, on the caller's stream of any kind."""
+    torch = pytest.importorskip("torch")
+    from horayzon_extpar_gb300.horizon_svf import horizon_svf_comp_batch, horizon_svf_comp_device
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    h0, s0, st0 = horizon_svf_comp_py(*small_domain.inputs(), *args, direct_launch=True,
+                                      return_stats=True)
+    for _ in range(2):  # first call instantiates, the second updates
+        h1, s1, st1 = horizon_svf_comp_py(*small_domain.inputs(), *args, return_stats=True)
+        np.testing.assert_array_equal(h0, h1)
+        np.testing.assert_array_equal(s0, s1)
+        assert st0["num_rays"] == st1["num_rays"]
+    # Another shape (refinement), then back.
+    args2 = (24, 1, 40000.0, 0.2, 3, 1)
+    h2, s2 = horizon_svf_comp_py(*small_domain.inputs(), *args2, direct_launch=True)
+    h3, s3 = horizon_svf_comp_py(*small_domain.inputs(), *args2)
+    np.testing.assert_array_equal(h2, h3)
+    np.testing.assert_array_equal(s2, s3)
+    # Device entry on torch's default stream and on a side stream.
+    t = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in small_domain.inputs()]
+    hd, sd, _ = horizon_svf_comp_device(*t, *args)
+    np.testing.assert_array_equal(hd.cpu().numpy(), h0)
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        he, se, _ = horizon_svf_comp_device(*t, *args, stream=side)
+    side.synchronize()
+    np.testing.assert_array_equal(he.cpu().numpy(), h0)
+    np.testing.assert_array_equal(se.cpu().numpy(), s0)
+    # Batch of two domains.
+    other = synthetic.make_domain(edge_km=3.0, box_km=50.0, seed=11)
+    doms = [(small_domain.inputs(), args), (other.inputs(), args2)]
+    ref = horizon_svf_comp_batch(doms, direct_launch=True)
+    got = horizon_svf_comp_batch(doms)
+    for (ha, sa), (hb, sb) in zip(ref, got):
+        np.testing.assert_array_equal(ha, hb)
+        np.testing.assert_array_equal(sa, sb)
