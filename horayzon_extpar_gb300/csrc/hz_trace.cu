@@ -15,6 +15,8 @@
 //   * clip at 0, sector mean over refine_factor, rad->deg and the SVF sum
 //     (cpp:736-754, 333-358) accumulated online per azimuth, in the
 //     reference's summation order.
+#include <algorithm>
+
 #include "hz_internal.h"
 
 namespace hz {
@@ -505,10 +507,11 @@ __device__ __forceinline__ int domain_of(const DomainDesc* __restrict__ doms, in
 }
 
 // One step of a cell's bracketing search (mo_lradtopo_horayzon.cpp:490-555,
-// 694-754) on the state `st` (FP64: 0-2 sphere normal U, 3-5 north N, 6-8
-// east E, 9-11 horizontal direction of the current azimuth, 12 elevation
-// accumulator, 13 sector sum, 14 SVF sum; integers: domain, cell, azimuth,
-// phase, upward steps, lattice index m; FP32 ray origin hi and lo). Given the
+// 694-754) on the state `st` (FP64: 0-2 sphere normal U, 3-5 horizontal
+// direction of the current azimuth, 6 elevation accumulator, 7 sector sum,
+// 8 SVF sum; integers: domain, cell, azimuth, phase, upward steps, lattice
+// index m, work position; FP32 ray origin hi and lo). North and east are read
+// from the cell frame table at each new azimuth. Given the
 // result of the cell's last ray (or, in phase kPhaseStart, the work id k_new
 // of a new cell), it continues the bracket, or closes the azimuth (clip,
 // sector mean, SVF) and starts the next one, or finishes the cell. Returns 1
@@ -541,8 +544,6 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       const long long nc = D.ncell;
       const double* fr = D.cell_frame + p;
       SV(0) = fr[0]; SV(1) = fr[nc]; SV(2) = fr[2 * nc];
-      SV(3) = fr[3 * nc]; SV(4) = fr[4 * nc]; SV(5) = fr[5 * nc];
-      SV(6) = fr[6 * nc]; SV(7) = fr[7 * nc]; SV(8) = fr[8 * nc];
       const float* org = D.cell_origin + p;
       SO(0) = org[0];
       SO(1) = org[nc];
@@ -552,7 +553,7 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
         SO(4) = org[4 * nc];
         SO(5) = org[5 * nc];
       }
-      SV(12) = 0.0; SV(13) = 0.0; SV(14) = 0.0;
+      SV(6) = 0.0; SV(7) = 0.0; SV(8) = 0.0;
       a = 0;
       m = 0;
       phase = kPhaseFirst;
@@ -560,7 +561,7 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       // Result of the last ray: continue the bracket or close the azimuth.
       const DomainDesc& D = doms[dom];
       const double ha = D.hori_acc;
-      double elev = SV(12);
+      double elev = SV(6);
       if (phase == kPhaseFirst) {
         phase = last_hit ? kPhaseUp : kPhaseDown;
         up = 0;
@@ -576,7 +577,7 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
           m--;
           elev -= D.two_ha;
         }
-        SV(12) = elev;
+        SV(6) = elev;
         emit = true;
         break;
       }
@@ -585,7 +586,7 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       const int j = phase == kPhaseUp ? 2 * m - 1 : 2 * m + 1;  // h ~ j * ha
       if (D.raw_j) D.raw_j[(long long)a * D.ncell + cell] = (int16_t)j;
       if (h < 0.0) h = 0.0;
-      double sector = SV(13) + h;
+      double sector = SV(7) + h;
       if (D.refine == 1 || (a + 1) % D.refine == 0) {
         // Converted to degrees by k_finish_outputs.
         D.horizon[(long long)(D.refine == 1 ? a : a / D.refine) * D.ncell + cell] = sector;
@@ -594,7 +595,7 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       // SVF sum (cpp:333-358, 754). With refine_factor 1 the horizon array
       // holds every clipped h, and k_finish_outputs sums the SVF from it in
       // the same order.
-      double svf = SV(14);
+      double svf = SV(8);
       if (D.refine != 1) {
         double s = 0.0;
         if (h > 0.0) s = (j > 0 && j < kSinTable) ? __ldg(&D.sin_lattice[j]) : sin(h);
@@ -616,8 +617,8 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
         phase = kPhaseStart;
         break;
       }
-      SV(13) = sector;
-      SV(14) = svf;
+      SV(7) = sector;
+      SV(8) = svf;
       phase = kPhaseFirst;
     }
     // New azimuth: the elevation carries over (cpp:511), or starts at the
@@ -625,12 +626,15 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
     const int16_t* start_m = doms[dom].start_m;
     if (start_m && (a == 0 || doms[dom].start_all)) {
       m = start_m[(long long)a * doms[dom].ncell + cell];
-      SV(12) = (double)m * doms[dom].two_ha;
+      SV(6) = (double)m * doms[dom].two_ha;
     }
     const double2 cs = __ldg(&doms[dom].azim_cs[a]);
-    SV(9) = cs.x * SV(3) + cs.y * SV(6);
-    SV(10) = cs.x * SV(4) + cs.y * SV(7);
-    SV(11) = cs.x * SV(5) + cs.y * SV(8);
+    // North and east from the frame table (once per azimuth).
+    const long long nc = doms[dom].ncell;
+    const double* fr = doms[dom].cell_frame + p;
+    SV(3) = cs.x * fr[3 * nc] + cs.y * fr[6 * nc];
+    SV(4) = cs.x * fr[4 * nc] + cs.y * fr[7 * nc];
+    SV(5) = cs.x * fr[5 * nc] + cs.y * fr[8 * nc];
     emit = true;
   }
   st.i(3) = phase;
@@ -651,9 +655,9 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
     const double e = (double)m * D.two_ha;
     ecs = make_double2(cos(e), sin(e));
   }
-  dir.x = (float)(ecs.x * SV(9) + ecs.y * SV(0));
-  dir.y = (float)(ecs.x * SV(10) + ecs.y * SV(1));
-  dir.z = (float)(ecs.x * SV(11) + ecs.y * SV(2));
+  dir.x = (float)(ecs.x * SV(3) + ecs.y * SV(0));
+  dir.y = (float)(ecs.x * SV(4) + ecs.y * SV(1));
+  dir.z = (float)(ecs.x * SV(5) + ecs.y * SV(2));
   dom_out = dom;
   return 1;
 #undef SV
@@ -676,15 +680,15 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     k_trace_warp(const DomainDesc* __restrict__ doms, int ndom, const int* __restrict__ order,
                  int total, int* __restrict__ work, unsigned long long* __restrict__ counters,
                  int* __restrict__ err, int advance_min, int leaf_min, int chunk) {
-  // Per-lane search state. FP64: 0-2 sphere normal U, 3-5 north N, 6-8 east
-  // E, 9-11 horizontal direction of the current azimuth, 12 elevation
-  // accumulator, 13 sector sum, 14 SVF sum. Integers: domain, cell, azimuth,
-  // phase, upward steps, lattice index m of the current elevation, position
-  // of the cell in the work order. FP32 ray origin (hi, and lo in precise
-  // mode).
-  __shared__ double sv[15][kFlatBlock];
+  // Per-lane search state (112 bytes; the rest of the SM's L1 caches the
+  // tree). FP64: 0-2 sphere normal U, 3-5 horizontal direction of the
+  // current azimuth, 6 elevation accumulator, 7 sector sum, 8 SVF sum.
+  // Integers: domain, cell, azimuth, phase, upward steps, lattice index m of
+  // the current elevation, position of the cell in the work order. FP32 ray
+  // origin (hi, and lo in precise mode).
+  __shared__ double sv[9][kFlatBlock];
   __shared__ int si[7][kFlatBlock];
-  __shared__ float so[6][kFlatBlock];
+  __shared__ float so[kPrecise ? 6 : 3][kFlatBlock];
   __shared__ int wq[2][kFlatBlock / 32];  // per warp: next and end of its chunk of work ids
   constexpr unsigned kFull = 0xffffffffu;
   const int t = threadIdx.x;
@@ -791,8 +795,8 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
         tris = D.tris;
         if (kPrecise) tri_lo = D.tri_lo;
         if (kPrecise)
-          r = make_ray(so[0][t], so[1][t], so[2][t], d.x, d.y, d.z, D.tfar, so[3][t], so[4][t],
-                       so[5][t]);
+          r = make_ray(so[0][t], so[1][t], so[2][t], d.x, d.y, d.z, D.tfar,
+                       so[kPrecise ? 3 : 0][t], so[kPrecise ? 4 : 0][t], so[kPrecise ? 5 : 0][t]);
         else
           r = make_ray(so[0][t], so[1][t], so[2][t], d.x, d.y, d.z, D.tfar);
         ref = D.root;
@@ -1067,11 +1071,42 @@ cudaError_t cell_order(const double* cell_enu, int begin, int count, int id_offs
   return radix_sort_pairs(keys, order, keys_alt, vals_alt, count, 32, sort_scratch, s);
 }
 
+#ifndef HZ_CARVEOUT
+#define HZ_CARVEOUT 1  // 1: ask for the smallest shared-memory carveout that holds the blocks
+#endif
+
+// Shared memory is carved out of the SM's 256 KB of L1: ask for just what
+// HZ_WARP_MIN_BLOCKS resident blocks need, so the rest caches the tree.
+template <typename K>
+void prefer_l1(K kernel) {
+#if HZ_CARVEOUT
+  cudaFuncAttributes fa;
+  int dev = 0, smem_sm = 0, reserved = 0;
+  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) !=
+          cudaSuccess ||
+      cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) !=
+          cudaSuccess ||
+      smem_sm <= 0) {
+    (void)cudaGetLastError();
+    return;
+  }
+  const long long need = (long long)HZ_WARP_MIN_BLOCKS * ((long long)fa.sharedSizeBytes + reserved);
+  const int pct = (int)std::min<long long>(100, (need * 100 + smem_sm - 1) / smem_sm);
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct) !=
+      cudaSuccess)
+    (void)cudaGetLastError();
+#else
+  (void)kernel;
+#endif
+}
+
 // One persistent launch: as many blocks as fit on the device at once, at
 // most one block per kFlatBlock work items.
 template <typename... P, typename... A>
 cudaError_t launch_persistent(void (*kernel)(P...), int total, cudaStream_t s, A... args) {
   int dev = 0, sms = 0, per_sm = 0;
+  prefer_l1(kernel);
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kFlatBlock, 0);
