@@ -883,6 +883,8 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
               const hz_options& opt, hz_stats* stats) {
   auto t0 = std::chrono::steady_clock::now();
   if (n < 1) return fail(HZ_ERR_VALUE, "no domains");
+  // The search packs the domain index of a cell in 16 bits.
+  if (n > 65535) return fail(HZ_ERR_VALUE, "at most 65535 domains per call");
   long long total_cells = 0;
   for (int d = 0; d < n; d++) {
     const hz_domain& h = doms[d];

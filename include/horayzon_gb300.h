@@ -220,8 +220,9 @@ typedef struct hz_domain {
  * Many independent domains in one call: mesh, frames and BVH per domain
  * (each BVH in its own slice of one device arena), then ONE persistent
  * search launch over the cells of all domains. Every domain carries its own
- * arguments (num_hori, grid_type, ...). on_device = 0: host arrays (copied
- * in and out); on_device = 1: device arrays, work enqueued on `stream`. No
+ * arguments (num_hori, grid_type, ...); 1 <= n_domains <= 65535. on_device
+ * = 0: host arrays (copied in and out); on_device = 1: device arrays, work
+ * enqueued on `stream`. No
  * reference counterpart: the reference computes one domain per call
  * (mo_lradtopo_horayzon.cpp:562-785).
  */
