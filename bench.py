@@ -336,6 +336,46 @@ def batch_report(args):
             "kernel_launches": st["kernel_launches"]}
 
 
+def configs_report(dom, d_in, stream, reps=2):
+    """The other configurations of the workload family, device-resident
+    inputs, plain search: the 2.5 km / 400 km, 1 km / 1000 km and 100 m /
+    150 km grids at nhori 24, and the 500 m domain at nhori 48, at
+    refine_factor 10 and with grid_type 0. One evaluation is one (cell,
+    azimuth) of the output (refine_factor 10 traces ten azimuths per
+    evaluation)."""
+    import torch
+    from horayzon_extpar_gb300 import horizon_svf_comp_device, synthetic
+    runs = [("c1", "2.5 km grid, 400x400 km, nhori 24", None, ARGS),
+            ("c2", "1 km grid, 1000x1000 km, nhori 24", None, ARGS),
+            ("c4", "100 m grid, 150x150 km, nhori 24", None, ARGS),
+            ("c3_nhori48", "500 m grid, 600x600 km, nhori 48", dom, (48,) + ARGS[1:]),
+            ("c3_refine10", "500 m grid, 600x600 km, nhori 24, refine_factor 10", dom,
+             ARGS[:4] + (10, ARGS[5])),
+            ("c3_grid_type0", "500 m grid, 600x600 km, nhori 24, grid_type 0", dom,
+             (ARGS[0], 0) + ARGS[2:])]
+    out = {}
+    for key, desc, d, args in runs:
+        if d is None:
+            d = synthetic.make_config(key, seed=0)
+            t = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in d.inputs()]
+        else:
+            t = d_in
+        horizon_svf_comp_device(*t, *args, stream=stream)  # warm-up
+        best = None
+        for _ in range(reps):
+            _, _, st = horizon_svf_comp_device(*t, *args, stream=stream)
+            if best is None or st["ms_trace"] < best["ms_trace"]:
+                best = st
+        evals = d.ncell * args[0]
+        call_ms = best["ms_mesh"] + best["ms_bvh"] + best["ms_trace"]
+        out[key] = {"workload": desc, "ncell": d.ncell, "n_tri": best["n_tri"],
+                    "evals": evals, "search_ms": best["ms_trace"], "call_ms": call_ms,
+                    "evals_per_s_search": evals / (best["ms_trace"] * 1e-3),
+                    "evals_per_s_call": evals / (call_ms * 1e-3),
+                    "rays_per_eval": best["num_rays"] / evals}
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -483,6 +523,7 @@ def run_gpu(args):
         extras["precision"] = precision_report(dom, d_in, hz, sv, stream)
         extras["batched_domains"] = batch_report(args)
         extras["drop_in_numpy"] = drop_in_report(dom, min(args.steps, 3))
+        extras["configs"] = configs_report(dom, d_in, stream)
 
     peak, peak_kind = measured_peaks()
     alg_bytes = BYTES_PER_NODE * st_count["node_visits"] + BYTES_PER_TRI * st_count["tri_tests"]
