@@ -41,9 +41,34 @@ def _int_arg(v):
     return int(v)
 
 
+def _scalar_error(num_hori, grid_type, dist_search, ray_org_elev, refine_factor, svf_type):
+    """The first failing range check of horizon_svf.pyx:91-103, or None."""
+    if (num_hori < 4) or (num_hori > 1440):
+        return ValueError("'num_hori' must be in the range [4, 1440]")
+    if (grid_type < 0) or (grid_type > 1):
+        return ValueError("'grid_type' must be in the range [0, 1]")
+    if (dist_search < 1_000.0) or (dist_search > 500_000.0):
+        return ValueError("'dist_search' must be in the range "
+                          + "[1'000, 500'000] km")
+    if ray_org_elev < 0.1:
+        return TypeError("Minimal allowed value for 'ray_org_elev' is 0.1 m")
+    if (refine_factor < 1) or (refine_factor > 50):
+        return ValueError("'refine_factor' must be in the range [1, 50]")
+    if (svf_type < 0) or (svf_type > 2):
+        return ValueError("'svf_type' must be in the range [0, 2]")
+    return None
+
+
 def _check_args(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_type,
                 dist_search, ray_org_elev, refine_factor, svf_type):
-    """horizon_svf.pyx:78-103, same order, types and messages."""
+    """horizon_svf.pyx:78-103, same order, types and messages.
+
+    The index check of cells_of_vertex (pyx:88-90) is also made by the GPU
+    mesh stage, with the same condition, exception and message; it runs
+    here only where its place in the order of checks shows (another
+    argument is invalid, or an array is empty), and is otherwise left to the
+    GPU (a numpy pass over 6 x nvertex entries costs ~10 ms per call on
+    the benchmark domain)."""
     if (clon.size != clat.size) or (clat.size != hsurf.size):
         raise ValueError("Inconsistent lengths of input arrays 'clon', "
                          "'clat' and 'hsurf'")
@@ -53,22 +78,14 @@ def _check_args(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_t
     if cells_of_vertex.shape[0] != 6:
         raise ValueError("First dimension of 'cells_of_vertex' must "
                          + "have length 6")
-    if not np.all((cells_of_vertex >= 0) & (cells_of_vertex <= clon.size - 1)
-                  | (cells_of_vertex == -2)):
-        raise ValueError("Indices of 'cells_of_vertex' out of range")
-    if (num_hori < 4) or (num_hori > 1440):
-        raise ValueError("'num_hori' must be in the range [4, 1440]")
-    if (grid_type < 0) or (grid_type > 1):
-        raise ValueError("'grid_type' must be in the range [0, 1]")
-    if (dist_search < 1_000.0) or (dist_search > 500_000.0):
-        raise ValueError("'dist_search' must be in the range "
-                         + "[1'000, 500'000] km")
-    if ray_org_elev < 0.1:
-        raise TypeError("Minimal allowed value for 'ray_org_elev' is 0.1 m")
-    if (refine_factor < 1) or (refine_factor > 50):
-        raise ValueError("'refine_factor' must be in the range [1, 50]")
-    if (svf_type < 0) or (svf_type > 2):
-        raise ValueError("'svf_type' must be in the range [0, 2]")
+    err = _scalar_error(num_hori, grid_type, dist_search, ray_org_elev, refine_factor,
+                        svf_type)
+    if err is not None or clon.size == 0 or vlon.size == 0:
+        if not np.all((cells_of_vertex >= 0) & (cells_of_vertex <= clon.size - 1)
+                      | (cells_of_vertex == -2)):
+            raise ValueError("Indices of 'cells_of_vertex' out of range")
+    if err is not None:
+        raise err
 
 
 def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,

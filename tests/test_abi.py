@@ -71,13 +71,16 @@ def test_array_checks_match_reference(dom):
         horizon_svf_comp_py(*c[:3], c[3][:-1], *c[4:], *ARGS)
     with pytest.raises(ValueError, match="First dimension of 'cells_of_vertex' must have length 6"):
         horizon_svf_comp_py(*c[:5], c[5][:5], *ARGS)
+    # The index check comes before the range checks of the scalar arguments
+    # (pyx:88-90 before :91-103); with a valid call the GPU makes it
+    # (test_gpu_parity.test_gpu_bad_indices_raise_reference_error).
     bad = c[5].copy()
     bad[0, 0] = dom.ncell
     with pytest.raises(ValueError, match="Indices of 'cells_of_vertex' out of range"):
-        horizon_svf_comp_py(*c[:5], bad, *ARGS)
+        horizon_svf_comp_py(*c[:5], bad, 3, *ARGS[1:])
     bad[0, 0] = -1
     with pytest.raises(ValueError, match="Indices of 'cells_of_vertex' out of range"):
-        horizon_svf_comp_py(*c[:5], bad, *ARGS)
+        horizon_svf_comp_py(*c[:5], bad, *ARGS[:5], 7)
     with pytest.raises(ValueError, match="Buffer dtype mismatch"):
         horizon_svf_comp_py(c[0].astype(np.float32), *c[1:], *ARGS)
     with pytest.raises(ValueError, match="Buffer dtype mismatch"):

@@ -320,3 +320,16 @@ def test_gpu_graph_replay_matches_direct_launch(small_domain):
     for (ha, sa), (hb, sb) in zip(ref, got):
         np.testing.assert_array_equal(ha, hb)
         np.testing.assert_array_equal(sa, sb)
+
+
+@pytest.mark.parametrize("value", ["ncell", -1, -3])
+def test_gpu_bad_indices_raise_reference_error(small_domain, value):
+    """With every other argument valid, the index check of cells_of_vertex
+    (pyx:88-90) is the GPU mesh stage's: same exception and message."""
+    c = small_domain.inputs()
+    bad = c[5].copy()
+    bad[3, 17] = small_domain.ncell if value == "ncell" else value
+    with pytest.raises(ValueError, match="Indices of 'cells_of_vertex' out of range$"):
+        horizon_svf_comp_py(*c[:5], bad, 24, 1, 40000.0, 0.2, 1, 2)
+    h, s = horizon_svf_comp_py(*c, 24, 1, 40000.0, 0.2, 1, 2)
+    assert np.isfinite(h).all()
