@@ -370,33 +370,62 @@ constexpr int kFlatBlock = 128;
 enum : int { kPhaseStart = 0, kPhaseFirst = 1, kPhaseUp = 2, kPhaseDown = 3 };
 
 #ifndef HZ_STACK_TOP
-#define HZ_STACK_TOP 1  // 1: the top stack entry lives in a register
+#define HZ_STACK_TOP 1  // 1: the top stack entries live in registers (StackTop)
 #endif
 // Traversal stack: entries in `stack` (local memory) below a top entry held
 // in a register (kEmptyRef when the stack is empty), so that a pop returns at
 // once and the reload of the next top overlaps with the node fetch.
-__device__ __forceinline__ void stk_push(int* stack, int& sp, int& top, int x) {
-#if HZ_STACK_TOP
-  if (top != kEmptyRef) stack[sp++] = top;
-  top = x;
-#else
-  stack[sp++] = x;
-#endif
+// The top entries of a traversal stack held in registers: `a` is the top,
+// `b` the entry below it (kRegs == 2 only; empty while `a` is); the rest
+// lives in local memory, stack[0, sp). The binary tree pushes and pops once
+// per visit and gains from two register entries; the 4-wide tree, which
+// pushes up to three children at once, from one (HZ_STACK_TOP 0: none).
+struct StackTop {
+  int a = kEmptyRef;
+  int b = kEmptyRef;
+  __device__ void clear() {
+    a = kEmptyRef;
+    b = kEmptyRef;
+  }
+};
+template <int kRegs>
+__device__ __forceinline__ void stk_push(int* stack, int& sp, StackTop& top, int x) {
+  if (HZ_STACK_TOP && kRegs == 2) {
+    if (top.b != kEmptyRef) stack[sp++] = top.b;
+    top.b = top.a;
+    top.a = x;
+  } else if (HZ_STACK_TOP) {
+    if (top.a != kEmptyRef) stack[sp++] = top.a;
+    top.a = x;
+  } else {
+    stack[sp++] = x;
+  }
 }
-__device__ __forceinline__ int stk_pop(int* stack, int& sp, int& top) {
-#if HZ_STACK_TOP
-  const int r = top;
-  top = sp > 0 ? stack[--sp] : kEmptyRef;
-  return r;
-#else
+template <int kRegs>
+__device__ __forceinline__ int stk_pop(int* stack, int& sp, StackTop& top) {
+  if (HZ_STACK_TOP && kRegs == 2) {
+    const int r = top.a;
+    if (top.b != kEmptyRef) {
+      top.a = top.b;
+      top.b = kEmptyRef;
+    } else {
+      top.a = sp > 0 ? stack[--sp] : kEmptyRef;
+    }
+    return r;
+  }
+  if (HZ_STACK_TOP) {
+    const int r = top.a;
+    top.a = sp > 0 ? stack[--sp] : kEmptyRef;
+    return r;
+  }
   return sp > 0 ? stack[--sp] : kEmptyRef;
-#endif
 }
+constexpr int kRegsBinary = 2, kRegsWide = 1;
 
 // Visits internal node `ref`: descends into the nearer hit child (pushing the
 // other), or pops. Returns false on stack overflow.
 __device__ __forceinline__ bool visit_node(const Node* __restrict__ nodes, const Ray& r,
-                                           int& ref, int* stack, int& sp, int& top) {
+                                           int& ref, int* stack, int& sp, StackTop& top) {
   const Node* nd = nodes + ref;
   const float4 na = __ldg(&nd->a);
   const float4 nb = __ldg(&nd->b);
@@ -409,14 +438,14 @@ __device__ __forceinline__ bool visit_node(const Node* __restrict__ nodes, const
   if (h0 && h1) {
     if (sp >= kStackDepth - 1) return false;
     const bool near0 = t0 <= t1;
-    stk_push(stack, sp, top, near0 ? c1 : c0);
+    stk_push<kRegsBinary>(stack, sp, top, near0 ? c1 : c0);
     ref = near0 ? c0 : c1;
   } else if (h0) {
     ref = c0;
   } else if (h1) {
     ref = c1;
   } else {
-    ref = stk_pop(stack, sp, top);
+    ref = stk_pop<kRegsBinary>(stack, sp, top);
   }
   return true;
 }
@@ -425,7 +454,7 @@ __device__ __forceinline__ bool visit_node(const Node* __restrict__ nodes, const
 // other hit children, farthest first; pops when no child is hit. Returns false
 // on stack overflow.
 __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, const Ray& r,
-                                            int& ref, int* stack, int& sp, int& top) {
+                                            int& ref, int* stack, int& sp, StackTop& top) {
   // Planes in node order lo.x, hi.x, lo.y, hi.y, lo.z, hi.z: the near plane
   // of an axis is lo + n (n = 1 for a negative inverse direction).
   const float4* pl = reinterpret_cast<const float4*>(nodes4 + ref);
@@ -462,14 +491,14 @@ __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, co
   cx(t1, r1, t2, r2);
 #endif
   if (t0 == INFINITY) {
-    ref = stk_pop(stack, sp, top);
+    ref = stk_pop<kRegsWide>(stack, sp, top);
     return true;
   }
   const int extra = (t1 != INFINITY) + (t2 != INFINITY) + (t3 != INFINITY);
   if (sp + extra >= kStackDepth4) return false;
-  if (t3 != INFINITY) stk_push(stack, sp, top, r3);
-  if (t2 != INFINITY) stk_push(stack, sp, top, r2);
-  if (t1 != INFINITY) stk_push(stack, sp, top, r1);
+  if (t3 != INFINITY) stk_push<kRegsWide>(stack, sp, top, r3);
+  if (t2 != INFINITY) stk_push<kRegsWide>(stack, sp, top, r2);
+  if (t1 != INFINITY) stk_push<kRegsWide>(stack, sp, top, r1);
   ref = r0;
   return true;
 }
@@ -702,7 +731,8 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   si[3][t] = kPhaseStart;
 
   bool alive = true, need = true, last_hit = false;
-  int ref = kEmptyRef, sp = 0, top = kEmptyRef;
+  int ref = kEmptyRef, sp = 0;
+  StackTop top;
   // Postponed leaf as next triangle << 4 | triangles left (0 = none).
   int pl0 = 0;
   int stack[kWide ? kStackDepth4 : kStackDepth];
@@ -727,7 +757,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   auto settle = [&]() {
     if (ref < 0 && ref != kEmptyRef && pl0 == 0) {
       pl0 = (leaf_start(ref) << 4) | leaf_count(ref);
-      ref = stk_pop(stack, sp, top);
+      ref = stk_pop<kWide ? kRegsWide : kRegsBinary>(stack, sp, top);
     }
     if (ref == kEmptyRef && pl0 == 0) {
       need = true;
@@ -801,7 +831,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
           r = make_ray(so[0][t], so[1][t], so[2][t], d.x, d.y, d.z, D.tfar);
         ref = D.root;
         sp = 0;
-        top = kEmptyRef;
+        top.clear();
         pl0 = 0;
         need = false;
         rays++;
