@@ -136,18 +136,23 @@ extern "C" int hz_distance_to_border(const double* clon, const double* clat,
   const double *d_clon = clon, *d_clat = clat, *d_vlon = vlon, *d_vlat = vlat;
   const int* d_cov = cells_of_vertex;
   double* d_dist = dist;
+  // The first failing call is reported (after the buffer is freed).
+  cudaError_t first = cudaSuccess;
+  auto ck = [&](cudaError_t r) {
+    if (first == cudaSuccess && r != cudaSuccess) first = r;
+  };
   if (!on_device) {
     double* a = (double*)take(nc * 8);
     double* b = (double*)take(nc * 8);
     double* c = (double*)take(nv * 8);
     double* d = (double*)take(nv * 8);
     int* cv = (int*)take(6 * nv * 4);
-    cudaMemcpyAsync(a, clon, nc * 8, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(b, clat, nc * 8, cudaMemcpyHostToDevice, s);
+    ck(cudaMemcpyAsync(a, clon, nc * 8, cudaMemcpyHostToDevice, s));
+    ck(cudaMemcpyAsync(b, clat, nc * 8, cudaMemcpyHostToDevice, s));
     if (num_vertex > 0) {
-      cudaMemcpyAsync(c, vlon, nv * 8, cudaMemcpyHostToDevice, s);
-      cudaMemcpyAsync(d, vlat, nv * 8, cudaMemcpyHostToDevice, s);
-      cudaMemcpyAsync(cv, cells_of_vertex, 6 * nv * 4, cudaMemcpyHostToDevice, s);
+      ck(cudaMemcpyAsync(c, vlon, nv * 8, cudaMemcpyHostToDevice, s));
+      ck(cudaMemcpyAsync(d, vlat, nv * 8, cudaMemcpyHostToDevice, s));
+      ck(cudaMemcpyAsync(cv, cells_of_vertex, 6 * nv * 4, cudaMemcpyHostToDevice, s));
     }
     d_clon = a;
     d_clat = b;
@@ -162,9 +167,9 @@ extern "C" int hz_distance_to_border(const double* clon, const double* clat,
   // Reference point of the domain for the FP32 sweep: the first cell.
   double lon0 = 0.0, lat0 = 0.0;
   if (on_device) {
-    cudaMemcpyAsync(&lon0, clon, 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&lat0, clat, 8, cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
+    ck(cudaMemcpyAsync(&lon0, clon, 8, cudaMemcpyDeviceToHost, s));
+    ck(cudaMemcpyAsync(&lat0, clat, 8, cudaMemcpyDeviceToHost, s));
+    ck(cudaStreamSynchronize(s));
   } else {
     lon0 = clon[0];
     lat0 = clat[0];
@@ -172,16 +177,19 @@ extern "C" int hz_distance_to_border(const double* clon, const double* clat,
   const double cl = std::cos(lat0);
   const double3 ref = make_double3((kRadE * cl) * std::cos(lon0), (kRadE * cl) * std::sin(lon0),
                                    kRadE * std::sin(lat0));
-  cudaMemsetAsync(count, 0, 4, s);
-  if (num_vertex > 0)
+  ck(cudaMemsetAsync(count, 0, 4, s));
+  if (num_vertex > 0) {
     k_border_collect<<<grid_for(num_vertex, 256), 256, 0, s>>>(d_vlon, d_vlat, d_cov,
                                                                num_vertex, ref, bv64, bv32,
                                                                count);
+    ck(cudaGetLastError());
+  }
   k_border_nearest<<<grid_for(num_cell, 256), 256, 0, s>>>(d_clon, d_clat, num_cell, ref, bv64,
                                                            bv32, count, d_dist);
-  if (!on_device) cudaMemcpyAsync(dist, d_dist, nc * 8, cudaMemcpyDeviceToHost, s);
-  e = cudaStreamSynchronize(s);
-  if (e == cudaSuccess) e = cudaGetLastError();
+  ck(cudaGetLastError());
+  if (!on_device) ck(cudaMemcpyAsync(dist, d_dist, nc * 8, cudaMemcpyDeviceToHost, s));
+  ck(cudaStreamSynchronize(s));
+  e = first;
   cudaFree(buf);
   if (e != cudaSuccess) {
     char msg[256];

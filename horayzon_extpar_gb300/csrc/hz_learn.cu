@@ -369,8 +369,9 @@ cudaError_t mlp_train_step(float* params, float* adam_m, float* adam_v, const fl
   float* G2 = G1 + (size_t)n * kHid;
   float* G3 = G2 + (size_t)n * kHid;
   float* Y = G3 + n;
-  cudaMemsetAsync(grads, 0, sizeof(float) * kMlpParams, s);
-  cudaMemsetAsync(loss, 0, sizeof(float), s);
+  cudaError_t e = cudaMemsetAsync(grads, 0, sizeof(float) * kMlpParams, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(loss, 0, sizeof(float), s);
+  if (e != cudaSuccess) return e;
   const size_t smem = sizeof(float) * kMlpParams;
   k_mlp_train_fwd_bwd<<<grid_for(n, 128), 128, smem, s>>>(params, X, T, n, H1, H2, G1, G2, G3,
                                                          Y, loss);

@@ -224,8 +224,11 @@ cudaError_t radix_sort_pairs(uint32_t* keys, int32_t* vals, uint32_t* keys_alt,
     int32_t* tv = vi; vi = vo; vo = tv;
   }
   if (ki != keys) {
-    cudaMemcpyAsync(keys, ki, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(vals, vi, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+    cudaError_t e =
+        cudaMemcpyAsync(keys, ki, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(vals, vi, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
 }
