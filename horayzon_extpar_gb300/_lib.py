@@ -25,7 +25,7 @@ EXPORTED_SYMBOLS = ("hz_default_options", "horizon_svf_comp", "horizon_svf_comp_
                     "hz_last_error", "hz_version", "hz_release_workspace",
                     "hz_horizon_svf_device_static", "hz_horizon_svf_batch",
                     "hz_mlp_num_params", "hz_mlp_train_step", "hz_mlp_forward",
-                    "hz_distance_to_border")
+                    "hz_distance_to_border", "hz_occluded32")
 
 
 class Domain(C.Structure):
@@ -123,6 +123,10 @@ def load(build_if_missing: bool = True):
         L.hz_horizon_svf_batch.restype = C.c_int
         L.hz_horizon_svf_batch.argtypes = [C.POINTER(Domain), C.c_int, C.c_int, C.c_void_p,
                                            C.POINTER(Options), C.POINTER(Stats)]
+        L.hz_occluded32.restype = C.c_int
+        L.hz_occluded32.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                    C.c_void_p, C.c_int, C.c_float, C.c_void_p, C.c_int,
+                                    C.c_int, C.c_int]
         L.hz_distance_to_border.restype = C.c_int
         L.hz_distance_to_border.argtypes = [C.c_void_p] * 5 + [C.c_int, C.c_int, C.c_void_p,
                                                                C.c_int, C.c_void_p]

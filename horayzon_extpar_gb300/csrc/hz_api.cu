@@ -1256,6 +1256,82 @@ int hz_build_mesh(const double* clon, const double* clat, const double* hsurf,
                           nullptr, cap_vert, vertex_of_triangle, cap_tri, n_mesh_vert, n_tri);
 }
 
+int hz_occluded32(const float* vert, int n_vert, const int32_t* vertex_of_triangle, int n_tri,
+                  const float* org, const float* dir, int n_ray, float tfar, uint8_t* hit,
+                  int tree, int leaf_size, int device) {
+  g_last_error.clear();
+  if (n_vert < 0 || n_tri < 0 || n_ray < 0 || (tree != 0 && tree != 1) ||
+      (n_vert > 0 && !vert) || (n_tri > 0 && !vertex_of_triangle) ||
+      (n_ray > 0 && (!org || !dir || !hit)))
+    return fail(HZ_ERR_VALUE, "invalid arguments");
+  if (n_tri >= (1 << 27)) return fail(HZ_ERR_VALUE, "more than 2^27 triangles");
+  for (long long k = 0; k < 3LL * n_tri; k++)
+    if (vertex_of_triangle[k] < 0 || vertex_of_triangle[k] >= n_vert)
+      return fail(HZ_ERR_INDEX, "vertex_of_triangle index out of range");
+  if (n_ray == 0) return HZ_OK;
+  Engine* E = nullptr;
+  int rc = get_engine(device, &E);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(E->mu);
+  HZ_CUDA(cudaSetDevice(E->device));
+  cudaStream_t s = E->stream;
+  const bool wide = tree == 0;
+  const long long nt = n_tri > 0 ? n_tri : 1;
+  auto carve = [&](Carver& c, float*& v, int*& t, float*& o, float*& d, uint8_t*& h, int*& err,
+                   Node*& nodes, Node4*& nodes4, Tri*& tris, BvhScratch& sc) {
+    v = c.take<float>(3LL * (n_vert > 0 ? n_vert : 1));
+    t = c.take<int>(3 * nt);
+    o = c.take<float>(3LL * n_ray);
+    d = c.take<float>(3LL * n_ray);
+    h = c.take<uint8_t>(n_ray);
+    err = c.take<int>(4);
+    nodes = c.take<Node>(nt > 1 ? nt - 1 : 1);
+    nodes4 = wide ? c.take<Node4>(nt > 1 ? nt - 1 : 1) : nullptr;
+    tris = c.take<Tri>(nt);
+    sc.keys = c.take<uint32_t>(nt);
+    sc.vals = c.take<int32_t>(nt);
+    sc.keys_alt = c.take<uint32_t>(nt);
+    sc.vals_alt = c.take<int32_t>(nt);
+    sc.cxy = c.take<float2>(nt);
+    sc.parent = c.take<int>(nt);
+    sc.nsize = c.take<int>(nt);
+    sc.counter = c.take<int>(nt);
+    sc.bounds = c.take<unsigned>(16);
+    sc.sort_scratch = c.take<char>(radix_scratch_u32(nt));
+  };
+  float *v, *o, *d;
+  int *t, *err;
+  uint8_t* h;
+  Node* nodes;
+  Node4* nodes4;
+  Tri* tris;
+  BvhScratch sc;
+  Carver dry(nullptr);
+  carve(dry, v, t, o, d, h, err, nodes, nodes4, tris, sc);
+  rc = E->reserve(dry.off, s);
+  if (rc) return rc;
+  Carver c(E->arena);
+  carve(c, v, t, o, d, h, err, nodes, nodes4, tris, sc);
+  if (n_vert > 0)
+    HZ_CUDA(copy_from_host(E->staging, v, vert, sizeof(float) * 3 * (size_t)n_vert, s));
+  if (n_tri > 0)
+    HZ_CUDA(copy_from_host(E->staging, t, vertex_of_triangle, sizeof(int) * 3 * (size_t)n_tri,
+                           s));
+  HZ_CUDA(copy_from_host(E->staging, o, org, sizeof(float) * 3 * (size_t)n_ray, s));
+  HZ_CUDA(copy_from_host(E->staging, d, dir, sizeof(float) * 3 * (size_t)n_ray, s));
+  HZ_CUDA(cudaMemsetAsync(err, 0, 4 * sizeof(int), s));
+  HZ_CUDA(bvh_build(v, t, n_tri, nodes, tris, sc, s, nullptr, nullptr, nodes4,
+                    leaf_size > 0 ? leaf_size : kLeafMax));
+  HZ_CUDA(trace_rays(nodes, nodes4, tris, n_tri > 0 ? 0 : kEmptyRef, o, d, n_ray, tfar, wide, h,
+                     err, s));
+  HZ_CUDA(copy_to_host(E->staging, hit, h, (size_t)n_ray, s));
+  int err_h = 0;
+  HZ_CUDA(cudaMemcpyAsync(&err_h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HZ_CUDA(cudaStreamSynchronize(s));
+  if (err_h & kErrStack) return fail(HZ_ERR_INTERNAL, "traversal stack overflow");
+  return HZ_OK;
+}
+
 int hz_mesh_enu32(const double* clon, const double* clat, const double* hsurf,
                   const double* vlon, const double* vlat, const int32_t* cells_of_vertex,
                   int num_cell, int num_vertex, int grid_type, float* enu32, int cap_vert,

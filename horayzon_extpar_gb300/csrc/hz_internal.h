@@ -113,6 +113,12 @@ cudaError_t trace_tables(double2* azim_cs, double2* elev_cs, double* sin_lattice
                          double shift, double hori_acc, cudaStream_t s);
 // One thread per cell, nested loops as in the reference (simple; kept as the
 // second implementation the flattened kernel is tested against).
+// Any-hit flags (hit[i] = 1) of n_ray rays (org, dir: float3 on the device)
+// against a tree built by bvh_build; wide: the 4-wide tree (nodes4), else
+// the binary one. One thread per ray.
+cudaError_t trace_rays(const Node* nodes, const Node4* nodes4, const Tri* tris, int root,
+                       const float* org, const float* dir, int n_ray, float tfar, bool wide,
+                       uint8_t* hit, int* err, cudaStream_t s);
 cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s);
 // Morton order of cells [begin, begin + count) into order[count]; also resets
 // the work counter used by trace_flat.

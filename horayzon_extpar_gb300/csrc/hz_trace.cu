@@ -911,6 +911,42 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   }
 }
 
+// Any-hit query of arbitrary rays, one thread per ray, with the search's own
+// ray setup, box tests, traversal steps and watertight triangle test
+// (mo_lradtopo_horayzon.cpp:446-460): the binary tree through `occluded`,
+// the 4-wide tree through visit_node4 and test_tri.
+template <bool kWide>
+__global__ void __launch_bounds__(128)
+    k_rays(const Node* __restrict__ nodes, const Node4* __restrict__ nodes4,
+           const Tri* __restrict__ tris, int root, const float* __restrict__ org,
+           const float* __restrict__ dir, int n, float tfar, uint8_t* __restrict__ hit,
+           int* __restrict__ err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Ray r = make_ray(org[3LL * i], org[3LL * i + 1], org[3LL * i + 2], dir[3LL * i],
+                         dir[3LL * i + 1], dir[3LL * i + 2], tfar);
+  bool h = false;
+  if (!kWide) {
+    unsigned long long nv = 0, nt = 0;
+    h = occluded<false>(r, nodes, tris, root, nv, nt, err);
+  } else {
+    int stack[kStackDepth4];
+    int sp = 0, ref = root;
+    StackTop top;
+    while (ref != kEmptyRef && !h) {
+      if (ref < 0) {
+        const int s0 = leaf_start(ref), c = leaf_count(ref);
+        for (int k = s0; k < s0 + c && !h; k++) h = test_tri<false>(tris, nullptr, r, k);
+        ref = stk_pop<kRegsWide>(stack, sp, top);
+      } else if (!visit_node4(nodes4, r, ref, stack, sp, top)) {
+        atomicOr(err, kErrStack);
+        h = true;
+      }
+    }
+  }
+  hit[i] = h ? 1 : 0;
+}
+
 // Frame and FP32 ray origin of every traced cell, mo_lradtopo_horayzon.cpp:
 // 694-720 (the per-cell kernel's expressions), stored by the cell's position
 // in the work order (the search reads them coalesced).
@@ -1196,6 +1232,20 @@ static cudaError_t launch_search(const DomainDesc* doms, int ndom, const int32_t
                     : launch_variant<false, false>(doms, ndom, order, total, work, counters,
                                                    err, k.advance_min, k.leaf_min, c, k.variant,
                                                    s);
+}
+
+cudaError_t trace_rays(const Node* nodes, const Node4* nodes4, const Tri* tris, int root,
+                       const float* org, const float* dir, int n_ray, float tfar, bool wide,
+                       uint8_t* hit, int* err, cudaStream_t s) {
+  if (n_ray <= 0) return cudaSuccess;
+  if (wide)
+    k_rays<true><<<grid_for(n_ray, 128), 128, 0, s>>>(nodes, nodes4, tris, root, org, dir,
+                                                      n_ray, tfar, hit, err);
+  else
+    k_rays<false><<<grid_for(n_ray, 128), 128, 0, s>>>(nodes, nodes4, tris, root, org, dir,
+                                                       n_ray, tfar, hit, err);
+  note_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s) {

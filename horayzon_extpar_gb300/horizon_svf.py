@@ -14,7 +14,8 @@ import numpy as np
 
 from . import _lib
 
-__all__ = ["horizon_svf_comp_py", "horizon_svf_comp_device", "build_mesh", "mesh_enu32"]
+__all__ = ["horizon_svf_comp_py", "horizon_svf_comp_device", "build_mesh", "mesh_enu32",
+           "occluded32"]
 
 _D = C.POINTER(C.c_double)
 _F = C.POINTER(C.c_float)
@@ -235,6 +236,26 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
                                  C.byref(st))
     _lib.check(rc)
     return horizon, skyview, st.as_dict()
+
+
+def occluded32(vert, vertex_of_triangle, org, dirs, tfar, *, tree=0, leaf_size=0, device=-1):
+    """Any-hit flags of FP32 rays against an FP32 triangle soup on the GPU
+    (the search's own query, mo_lradtopo_horayzon.cpp:446-460): ray i hits
+    when it meets a triangle at 0 < t <= tfar (t in units of |dirs[i]|).
+    ``tree``: 0 the 4-wide BVH of the persistent search, 1 the binary BVH."""
+    vert = np.ascontiguousarray(vert, dtype=np.float32).reshape(-1, 3)
+    vot = np.ascontiguousarray(vertex_of_triangle, dtype=np.int32).reshape(-1, 3)
+    org = np.ascontiguousarray(org, dtype=np.float32).reshape(-1, 3)
+    dirs = np.ascontiguousarray(dirs, dtype=np.float32).reshape(-1, 3)
+    if org.shape != dirs.shape:
+        raise ValueError("org and dirs must have the same shape")
+    hit = np.zeros(org.shape[0], dtype=np.uint8)
+    rc = _lib.load().hz_occluded32(vert.ctypes.data, vert.shape[0], vot.ctypes.data,
+                                   vot.shape[0], org.ctypes.data, dirs.ctypes.data,
+                                   org.shape[0], float(tfar), hit.ctypes.data, int(tree),
+                                   int(leaf_size), int(device))
+    _lib.check(rc)
+    return hit.astype(bool)
 
 
 def build_mesh(clon, clat, hsurf, vlon, vlat, cells_of_vertex, grid_type, device=-1):

@@ -230,6 +230,21 @@ int hz_horizon_svf_batch(hz_domain* domains, int n_domains, int on_device, void*
                          const hz_options* opt, hz_stats* stats);
 
 /*
+ * Any-hit occlusion of arbitrary rays against a triangle soup: the query the
+ * search makes for every ray (Embree's rtcOccluded1 with the reference's ray
+ * setup, mo_lradtopo_horayzon.cpp:446-460), built and traced with the same
+ * BVH build, box tests, traversal and watertight triangle test. vert: FP32
+ * [n_vert][3]; vertex_of_triangle: int32 [n_tri][3]; org, dir: FP32
+ * [n_ray][3] (dir need not be unit length); hit[i] = 1 when ray i meets a
+ * triangle at 0 < t <= tfar, t in units of |dir|. Host buffers. tree: 0 =
+ * the 4-wide BVH of the persistent search, 1 = the binary BVH; leaf_size:
+ * triangles per leaf (0 = 2). No reference counterpart as an entry point.
+ */
+int hz_occluded32(const float* vert, int n_vert, const int32_t* vertex_of_triangle, int n_tri,
+                  const float* org, const float* dir, int n_ray, float tfar, uint8_t* hit,
+                  int tree, int leaf_size, int device);
+
+/*
  * Triangle-mesh assembly alone (mo_lradtopo_horayzon.cpp:228-317), on the
  * GPU, host buffers: mesh vertex (lon, lat, elevation) for the cells followed
  * by the appended ICON vertices, and three vertex indices per triangle.
