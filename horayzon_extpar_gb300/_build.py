@@ -85,6 +85,33 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     return LIB_PATH
 
 
+def build_checked(out_dir: str) -> str:
+    """The library with device-side index checks (-DHZ_CHECKED=1) in out_dir;
+    returns its path. Load it through HZ_LIBRARY in a separate process."""
+    nvcc = nvcc_path()
+    os.makedirs(out_dir, exist_ok=True)
+    objs, procs = [], []
+    for src in sorted(glob.glob(os.path.join(CSRC, "*.cu"))):
+        obj = os.path.join(out_dir, os.path.basename(src)[:-3] + ".o")
+        objs.append(obj)
+        cmd = [nvcc, "-c", src, "-o", obj] + _flags() + ["-DHZ_CHECKED=1"]
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE,
+                                            stderr=subprocess.STDOUT, text=True)))
+    errors = []
+    for cmd, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            errors.append("%s\n%s" % (" ".join(cmd), out))
+    if errors:
+        raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
+    lib = os.path.join(out_dir, "libhorayzon_gb300.so")
+    r = subprocess.run([nvcc, "-shared", "-o", lib] + objs + ARCH + ["-lcudart_static"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
+    return lib
+
+
 PROBE_SRC = os.path.join(PKG, "probe", "hz_l2_probe.cu")
 PROBE_PATH = os.path.join(LIB_DIR, "libhz_probe.so")
 

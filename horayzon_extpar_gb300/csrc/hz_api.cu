@@ -705,6 +705,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.elev_floor = elev_floor;
       D.cell_offset = total - P.cell_begin;
       D.root = out->n_tri[d] > 0 ? 0 : kEmptyRef;
+      D.n_tri = out->n_tri[d];
       D.ncell = P.ncell;
       D.ncell_traced = P.cell_count;
       D.nhori = P.nhori;
@@ -737,7 +738,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   unsigned long long* rb = pin;  // words 0..15 (descriptors live beyond word 64)
   HZ_CUDA(cudaMemcpyAsync(rb + 8, bb.counters, 3 * sizeof(unsigned long long),
                           cudaMemcpyDeviceToHost, s));
-  HZ_CUDA(cudaMemcpyAsync(rb + 12, bb.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  HZ_CUDA(cudaMemcpyAsync(rb + 12, bb.err, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
   HZ_CUDA(cudaMemcpyAsync(rb + 14, bb.t0, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
   unsigned long long* rb_done = pin + 64;  // the totals / error slots are no longer needed
   if (n > 1)
@@ -755,8 +756,12 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   for (int k = 0; k < kCounterWords; k++) fprintf(stderr, " %llu", rb[32 + k]);
   fprintf(stderr, "\n");
 #endif
-  const int err1 = (int)(rb[12] & 0xFFFFFFFFull);
+  const int* errw = reinterpret_cast<const int*>(rb + 12);  // bit word, check code, index
+  const int err1 = errw[0];
   if (err1 & kErrStack) return fail(HZ_ERR_INTERNAL, "BVH traversal stack overflow");
+  if (err1 & kErrBounds)
+    return fail(HZ_ERR_INTERNAL, "bounds check failed in the search: check %d, index %d",
+                errw[1], errw[2]);
   if (n > 1)
     for (int d = 0; d < n; d++)
       out->latency_ms[d] = rb_done[2 * d + 1] > rb[14]

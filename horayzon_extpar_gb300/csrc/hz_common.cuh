@@ -25,7 +25,8 @@ constexpr int kMaxUpSteps = 720;            // one full turn of 0.5 deg steps
 enum : int {
   kErrBadIndex = 1,     // cells_of_vertex entry outside [0, ncell) and != -2
   kErrStack = 2,        // traversal stack overflow
-  kErrMeshCapacity = 4  // mesh emission beyond the sized buffers
+  kErrMeshCapacity = 4,  // mesh emission beyond the sized buffers
+  kErrBounds = 8         // checked builds (HZ_CHECKED): an index outside its array
 };
 
 // Leaf references are negative: ~(start << 3 | (count - 1)).

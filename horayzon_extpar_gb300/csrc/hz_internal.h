@@ -157,6 +157,7 @@ struct DomainDesc {
   double two_ha;              // 2 * hori_acc (exact): one elevation step
   long long cell_offset;      // work id of cell 0 of this domain
   int root, ncell, ncell_traced, nhori, refine, L, svf_type;
+  int n_tri;                  // triangles of the tree (nodes: max(1, n_tri - 1))
   float tfar;
 };
 

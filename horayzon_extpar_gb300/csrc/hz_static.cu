@@ -285,6 +285,7 @@ extern "C" int hz_horizon_svf_device_static(
   D.elev_floor = deg2rad_s(-85.0);
   D.cell_offset = 0;
   D.root = n_tri > 0 ? 0 : kEmptyRef;
+  D.n_tri = n_tri;
   D.ncell = num_cell;
   D.ncell_traced = num_cell;
   D.nhori = num_hori;
@@ -306,5 +307,6 @@ extern "C" int hz_horizon_svf_device_static(
                  "reading error word");
   HZ_STATIC_CUDA(cudaStreamSynchronize(s), "horizon search");
   if (err & kErrStack) return static_fail(HZ_ERR_INTERNAL, "BVH traversal stack overflow");
+  if (err & kErrBounds) return static_fail(HZ_ERR_INTERNAL, "bounds check failed in the search");
   return HZ_OK;
 }

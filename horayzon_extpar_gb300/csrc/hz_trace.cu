@@ -369,6 +369,31 @@ constexpr int kFlatBlock = 128;
 
 enum : int { kPhaseStart = 0, kPhaseFirst = 1, kPhaseUp = 2, kPhaseDown = 3 };
 
+#ifndef HZ_CHECKED
+#define HZ_CHECKED 0  // 1: the search checks its indices and records violations (kErrBounds)
+#endif
+// What a checked build checks: a node reference against the tree's nodes, a
+// leaf's triangle range against its triangles, an output row / cell.
+enum : int { kCheckNode = 1, kCheckLeaf = 2, kCheckOutput = 3 };
+
+// In checked builds: records the first failed check (code, index) in err[1],
+// err[2] and raises kErrBounds; the caller then skips the access. Without
+// HZ_CHECKED every check passes and compiles away.
+__device__ __forceinline__ bool check_ok(bool ok, int code, long long index, int* err) {
+#if HZ_CHECKED
+  if (!ok) {
+    if (atomicCAS(err + 1, 0, code) == 0) err[2] = (int)index;
+    atomicOr(err, kErrBounds);
+  }
+  return ok;
+#else
+  (void)code;
+  (void)index;
+  (void)err;
+  return true;
+#endif
+}
+
 #ifndef HZ_STACK_TOP
 #define HZ_STACK_TOP 1  // 1: the top stack entries live in registers (StackTop)
 #endif
@@ -550,7 +575,8 @@ __device__ __forceinline__ int domain_of(const DomainDesc* __restrict__ doms, in
 template <bool kPrecise, class S>
 __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __restrict__ doms,
                                            int ndom, const int* __restrict__ order, int total,
-                                           int k_new, bool last_hit, float3& dir, int& dom_out) {
+                                           int k_new, bool last_hit, float3& dir, int& dom_out,
+                                           int* err) {
 #define SV(k_) st.d(k_)
 #define SO(k_) st.f(k_)
   int dom = st.i(0), cell = st.i(1), a = st.i(2), phase = st.i(3), up = st.i(4), m = st.i(5);
@@ -618,7 +644,10 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       double sector = SV(7) + h;
       if (D.refine == 1 || (a + 1) % D.refine == 0) {
         // Converted to degrees by k_finish_outputs.
-        D.horizon[(long long)(D.refine == 1 ? a : a / D.refine) * D.ncell + cell] = sector;
+        const int row = D.refine == 1 ? a : a / D.refine;
+        if (check_ok(row < D.nhori && cell >= 0 && cell < D.ncell, kCheckOutput,
+                     (long long)row * D.ncell + cell, err))
+          D.horizon[(long long)row * D.ncell + cell] = sector;
         sector = 0.0;
       }
       // SVF sum (cpp:333-358, 754). With refine_factor 1 the horizon array
@@ -740,6 +769,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   const Node4* nodes4 = nullptr;
   const Tri* tris = nullptr;
   const float4* tri_lo = nullptr;
+  int n_tri = 0;  // of the lane's domain (checked builds)
   Ray r;
   unsigned long long rays = 0, nvis = 0, ntest = 0;
 #ifdef HZ_DIAG
@@ -756,7 +786,9 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   // leaf has missed.
   auto settle = [&]() {
     if (ref < 0 && ref != kEmptyRef && pl0 == 0) {
-      pl0 = (leaf_start(ref) << 4) | leaf_count(ref);
+      if (check_ok(leaf_start(ref) >= 0 && leaf_start(ref) + leaf_count(ref) <= n_tri,
+                   kCheckLeaf, leaf_start(ref), err))
+        pl0 = (leaf_start(ref) << 4) | leaf_count(ref);
       ref = stk_pop<kWide ? kRegsWide : kRegsBinary>(stack, sp, top);
     }
     if (ref == kEmptyRef && pl0 == 0) {
@@ -815,7 +847,8 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
       const LaneState st{sv, si, so, t};
       float3 d;
       int dom = 0;
-      const int res = search_step<kPrecise>(st, doms, ndom, order, total, k_new, last_hit, d, dom);
+      const int res =
+          search_step<kPrecise>(st, doms, ndom, order, total, k_new, last_hit, d, dom, err);
       if (res < 0) {
         alive = false;
       } else if (res > 0) {
@@ -823,6 +856,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
         if (kWide) nodes4 = D.nodes4;
         else nodes = D.nodes;
         tris = D.tris;
+        n_tri = D.n_tri;
         if (kPrecise) tri_lo = D.tri_lo;
         if (kPrecise)
           r = make_ray(so[0][t], so[1][t], so[2][t], d.x, d.y, d.z, D.tfar,
@@ -853,7 +887,11 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     for (int step = 0; step < HZ_NODE_STEPS; step++) {
       if (alive && !need && ref >= 0) {
         if (kCount) nvis++;
-        if (!(kWide ? visit_node4(nodes4, r, ref, stack, sp, top)
+        if (!check_ok(ref < (n_tri > 1 ? n_tri - 1 : 1), kCheckNode, ref, err)) {
+          ref = kEmptyRef;  // the ray ends as if it had hit (the call fails)
+          need = true;
+          last_hit = true;
+        } else if (!(kWide ? visit_node4(nodes4, r, ref, stack, sp, top)
                     : visit_node(nodes, r, ref, stack, sp, top))) {
           atomicOr(err, kErrStack);
           need = true;
