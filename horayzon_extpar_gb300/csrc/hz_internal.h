@@ -177,7 +177,7 @@ enum : int {
 };
 // Counter words of the search: 0 rays, 1 node visits, 2 triangle tests; with
 // -DHZ_DIAG, 3.. per-warp loop statistics (printed to stderr by the host).
-constexpr int kCounterWords = 16;
+constexpr int kCounterWords = 20;
 constexpr int kDefaultAdvanceMin = 12;
 constexpr int kDefaultLeafMin = 12;
 constexpr int kDefaultChunk = 32;

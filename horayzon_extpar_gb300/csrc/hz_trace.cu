@@ -777,8 +777,22 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   // passes, triangle lanes, advance passes, advancing lanes, live lanes,
   // tracing lanes (summed over iterations); warp start / end times.
   unsigned long long dg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  // SM clock cycles the warp spends in the advance, node and triangle
+  // sections of its loop.
+  unsigned long long cyc[3] = {0, 0, 0};
+  long long c_mark = clock64();
   unsigned long long t_start;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
+#define HZ_DIAG_SECTION(k_)              \
+  do {                                   \
+    const long long c_now_ = clock64();  \
+    cyc[k_] += c_now_ - c_mark;          \
+    c_mark = c_now_;                     \
+  } while (0)
+#else
+#define HZ_DIAG_SECTION(k_) \
+  do {                      \
+  } while (0)
 #endif
 
   // A leaf target is postponed when the lane holds none and the lane
@@ -873,6 +887,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
       }
     }
 
+    HZ_DIAG_SECTION(0);
     // Node pass.
 #ifdef HZ_DIAG
     {
@@ -901,6 +916,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
         }
       }
     }
+    HZ_DIAG_SECTION(1);
     // Triangle pass.
     const bool has_leaf = alive && !need && pl0 != 0;
     const unsigned pend = __ballot_sync(kFull, has_leaf);
@@ -925,6 +941,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
         }
       }
     }
+    HZ_DIAG_SECTION(2);
   }
   rays = warp_sum_u64(rays);
   if (kCount) {
@@ -945,9 +962,11 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     atomicMin(&counters[13], t_end);
     atomicMax(&counters[14], t_end);
     atomicAdd(&counters[15], t_end - t_start);
+    for (int q = 0; q < 3; q++) atomicAdd(&counters[16 + q], cyc[q]);
 #endif
   }
 }
+#undef HZ_DIAG_SECTION
 
 // Any-hit query of arbitrary rays, one thread per ray, with the search's own
 // ray setup, box tests, traversal steps and watertight triangle test
