@@ -120,7 +120,7 @@ cudaError_t trace_rays(const Node* nodes, const Node4* nodes4, const Tri* tris, 
                        const float* org, const float* dir, int n_ray, float tfar, bool wide,
                        uint8_t* hit, int* err, cudaStream_t s);
 cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s);
-// Morton order of cells [begin, begin + count) into order[count]; also resets
+// Hilbert-curve order of cells [begin, begin + count) into order[count]; also resets
 // the work counter used by trace_flat.
 // Work ids are id_offset + cell.
 size_t cell_order_scratch_bytes(long long n);

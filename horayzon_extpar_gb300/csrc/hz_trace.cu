@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(128) k_trace_exact(TraceParams p) {
 // queries). Same search and the same rays as k_trace_exact, restructured for
 // the SIMT machine:
 //   * persistent blocks take cells from a global counter in the order given
-//     by `order` (Morton order of the cells); each lane owns one cell at a
+//     by `order` (Hilbert-curve order of the cells); each lane owns one cell at a
 //     time and runs its bracketing search as a state machine;
 //   * every loop iteration is executed by all 32 lanes of a warp (the loop
 //     ends when no lane has work left), so the ballots see the whole warp;
@@ -825,7 +825,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     }
 #endif
     const bool advance = waiting != 0u && (__popc(waiting) >= advance_min || waiting == live);
-    // Cells for the lanes that start one: consecutive work ids (Morton order)
+    // Cells for the lanes that start one: consecutive work ids (curve order)
     // from the warp's chunk, refilled with one atomic of `chunk` ids.
     int k_new = 0;
     if (advance) {
@@ -1083,7 +1083,7 @@ __global__ void k_finish_outputs(const DomainDesc* __restrict__ doms, int ndom, 
   D.skyview[cell] = (svf_here ? svf : D.skyview[cell]) / (double)D.L;
 }
 
-// Morton keys (2 x 16 bits) of the traced cells' horizontal ENU position.
+// Bounds of the traced cells' horizontal ENU positions (for their curve keys).
 __global__ void k_cell_bounds(const double* __restrict__ cell_enu, int begin, int count,
                               unsigned* __restrict__ bounds) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1113,6 +1113,31 @@ __device__ __forceinline__ uint32_t spread16(uint32_t x) {
   return x;
 }
 
+#ifndef HZ_CELL_ORDER
+#define HZ_CELL_ORDER 1  // order of the work queue: 0 Morton (Z) curve, 1 Hilbert curve
+#endif
+
+// Index of (x, y) in [0, 2^16)^2 along the Hilbert curve (the classic
+// quadrant-by-quadrant construction, rotating / reflecting each sub-square).
+__device__ __forceinline__ uint32_t hilbert16(uint32_t x, uint32_t y) {
+  uint32_t d = 0;
+  for (uint32_t s = 1u << 15; s > 0; s >>= 1) {
+    const uint32_t rx = (x & s) ? 1u : 0u;
+    const uint32_t ry = (y & s) ? 1u : 0u;
+    d += s * s * ((3u * rx) ^ ry);
+    if (ry == 0) {
+      if (rx == 1) {
+        x = 65535u - x;
+        y = 65535u - y;
+      }
+      const uint32_t t = x;
+      x = y;
+      y = t;
+    }
+  }
+  return d;
+}
+
 __global__ void k_cell_keys(const double* __restrict__ cell_enu, int begin, int count,
                             int id_offset, const unsigned* __restrict__ bounds,
                             uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
@@ -1126,7 +1151,11 @@ __global__ void k_cell_keys(const double* __restrict__ cell_enu, int begin, int 
   const float fy = ey > 0.f ? (y - mny) * (65535.0f / ey) : 0.f;
   const uint32_t qx = fx <= 0.f ? 0u : (fx >= 65535.0f ? 65535u : (uint32_t)fx);
   const uint32_t qy = fy <= 0.f ? 0u : (fy >= 65535.0f ? 65535u : (uint32_t)fy);
+#if HZ_CELL_ORDER == 1
+  keys[k] = hilbert16(qx, qy);
+#else
   keys[k] = spread16(qx) | (spread16(qy) << 1);
+#endif
   vals[k] = id_offset + begin + k;
 }
 

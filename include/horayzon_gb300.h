@@ -73,7 +73,7 @@ typedef struct hz_options {
                                 postponed leaf before a triangle pass (1..32; 0 =
                                 library default) */
     int32_t leaf_size;       /* most triangles per BVH leaf (1..8; 0 = 2) */
-    int32_t queue_chunk;     /* persistent kernel: consecutive cells (Morton order) a
+    int32_t queue_chunk;     /* persistent kernel: consecutive cells (curve order) a
                                 warp takes from the work queue at a time (0 = 32) */
     int32_t direct_launch;   /* 1: launch every kernel directly instead of replaying a
                                 captured CUDA graph of the BVH build and search */
@@ -92,7 +92,7 @@ enum {
 };
 
 enum {
-    HZ_KERNEL_PERSISTENT = 0,  /* persistent search over Morton-ordered cells on a 4-wide
+    HZ_KERNEL_PERSISTENT = 0,  /* persistent search over Hilbert-ordered cells on a 4-wide
                                   BVH, warp-uniform loop, postponed leaves tested one
                                   triangle per pass */
     HZ_KERNEL_PER_CELL = 1,    /* one thread per cell, nested loops, binary BVH */
