@@ -7,8 +7,10 @@
 //   mesh_count + scan for every domain -> [read totals, check indices] ->
 //   mesh_emit + mesh_ecef for every domain -> [read cell ECEF sums] -> ENU
 //   frames on the host (glibc, same expressions as cpp:624-644) -> mesh_enu +
-//   bvh_build + lattice tables + Morton cell order for every domain -> ONE
-//   persistent search launch over all cells of all domains -> counters.
+//   bvh_build + lattice tables + cell order (Hilbert curve) for every domain
+//   -> cell-frame pre-pass, ONE persistent search launch over all cells of
+//   all domains, epilogue -> counters. The part after the host frames is
+//   captured into a CUDA graph kept on the engine (Capture).
 // Device memory comes from one grow-only arena per device, carved per call.
 #include <algorithm>
 #include <chrono>

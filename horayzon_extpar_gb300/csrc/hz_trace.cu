@@ -1,20 +1,25 @@
-// hz_trace.cu -- per-cell horizon search and SVF, one thread per ICON cell.
+// hz_trace.cu -- the horizon search and SVF over all cells, and the ray query.
 //
 // Replaces the tbb::parallel_reduce over cells (mo_lradtopo_horayzon.cpp:
 // 686-761), terrain_horizon (cpp:490-555) and its Embree occlusion queries
-// (cpp:446-460):
+// (cpp:446-460). Kernels: k_trace_warp, the persistent search (the default;
+// overview further down), with its pre-pass k_cell_frames and epilogue
+// k_finish_outputs; k_trace_exact, one thread per cell running the
+// reference's loops as written; k_rays, the any-hit query on arbitrary rays;
+// and the cell ordering and lattice tables. What they share:
 //   * the cell frame (sphere normal, north, ray origin) in FP64, cpp:694-722;
 //   * the chained bracketing search over L = nhori * refine_factor azimuths
-//     with the reference's incremental FP64 Rodrigues rotations (cpp:119-130)
-//     and its lattice of elevation steps (2 * 0.25 deg from 0, downward walk
-//     bounded by -85 deg), so the tested directions equal the reference's;
+//     on the reference's lattice of elevation steps (2 * 0.25 deg from 0,
+//     downward walk bounded by -85 deg): k_trace_exact with the reference's
+//     incremental FP64 Rodrigues rotations (cpp:119-130), the persistent
+//     search with each direction in closed form from tabulated lattice
+//     angles; both cast the same FP32 rays;
 //   * each ray as an FP32 any-hit query: conservative slab tests against the
-//     BVH2 node boxes and the watertight ray/triangle test of Woop, Benthin &
+//     node boxes (binary or 4-wide tree) and the watertight ray/triangle test of Woop, Benthin &
 //     Wald (JCGT 2013) with every operation explicitly rounded, so hit
 //     decisions are bit-identical to the CPU oracle's;
 //   * clip at 0, sector mean over refine_factor, rad->deg and the SVF sum
-//     (cpp:736-754, 333-358) accumulated online per azimuth, in the
-//     reference's summation order.
+//     (cpp:736-754, 333-358), in the reference's summation order.
 #include <algorithm>
 
 #include "hz_internal.h"
