@@ -333,3 +333,41 @@ def test_gpu_bad_indices_raise_reference_error(small_domain, value):
         horizon_svf_comp_py(*c[:5], bad, 24, 1, 40000.0, 0.2, 1, 2)
     h, s = horizon_svf_comp_py(*c, 24, 1, 40000.0, 0.2, 1, 2)
     assert np.isfinite(h).all()
+
+
+def _subdomain(d, keep_cells):
+    """Cells keep_cells of d with the vertices they use; cells_of_vertex
+    remapped (entries of dropped cells become -2)."""
+    keep_cells = np.asarray(keep_cells)
+    verts = np.unique(d.vertex_of_cell[:, keep_cells])
+    new_cell = np.full(d.ncell, -2, dtype=np.int64)
+    new_cell[keep_cells] = np.arange(keep_cells.size)
+    cov = d.cells_of_vertex[:, verts].astype(np.int64)
+    cov = np.where(cov >= 0, new_cell[np.maximum(cov, 0)], -2).astype(np.int32)
+    return (d.clon[keep_cells].copy(), d.clat[keep_cells].copy(), d.hsurf[keep_cells].copy(),
+            d.vlon[verts].copy(), d.vlat[verts].copy(), np.ascontiguousarray(cov))
+
+
+@pytest.mark.parametrize("ncell", [1, 2, 3, 17])
+def test_gpu_few_cell_domains(ncell):
+    d = synthetic.make_domain(edge_km=2.5, box_km=20.0, seed=6)
+    rng = np.random.default_rng(ncell)
+    first = int(rng.integers(0, d.ncell - ncell))
+    inputs = _subdomain(d, np.arange(first, first + ncell))
+    for grid_type in (0, 1):
+        for kernel in (0, 1, 2):
+            args = (16, grid_type, 20000.0, 0.5, 2, 1)
+            h, s = horizon_svf_comp_py(*inputs, *args, kernel=kernel)
+            ho, so, _ = oracle.horizon_svf(*inputs, *args)
+            np.testing.assert_array_equal(h, ho)
+            np.testing.assert_allclose(s, so, rtol=0, atol=1e-12)
+
+
+def test_gpu_cell_ranges_at_the_ends(small_domain):
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    h, s = horizon_svf_comp_py(*small_domain.inputs(), *args)
+    n = small_domain.ncell
+    for b, e in ((0, 1), (n - 1, n), (0, n), (5, 6)):
+        hr, sr = horizon_svf_comp_py(*small_domain.inputs(), *args, cells=(b, e))
+        np.testing.assert_array_equal(hr[:, b:e], h[:, b:e])
+        np.testing.assert_array_equal(sr[b:e], s[b:e])
