@@ -9,7 +9,7 @@ decision is the watertight test's):
   together;
 * ``leaf_min``: lanes of a warp that must hold a postponed leaf before a
   triangle pass runs;
-* ``queue_chunk``: consecutive cells (Morton order) a warp takes from the
+* ``queue_chunk``: consecutive cells (curve order) a warp takes from the
   work queue at a time;
 * ``kernel``: the 4-wide or the binary BVH.
 
