@@ -33,10 +33,33 @@ def case(seed):
 
 @pytest.mark.parametrize("seed", range(24))
 def test_gpu_random_configuration_matches_oracle(seed):
+    """Host entry, device entry or a two-domain batch (by seed), with the
+    4-wide, binary or per-cell search (by seed)."""
     dkw, args = case(seed)
     d = synthetic.make_domain(**dkw)
-    h, s, st = horizon_svf_comp_py(*d.inputs(), *args, return_stats=True)
+    kernel = (0, 2, 1)[seed % 3]
+    entry = seed % 4
     ho, so, sto = oracle.horizon_svf(*d.inputs(), *args)
+    if entry == 1:
+        torch = pytest.importorskip("torch")
+        from horayzon_extpar_gb300 import horizon_svf_comp_device
+        t = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in d.inputs()]
+        h, s, st = horizon_svf_comp_device(*t, *args, kernel=kernel)
+        h, s = h.cpu().numpy(), s.cpu().numpy()
+    elif entry == 2:
+        from horayzon_extpar_gb300.horizon_svf import horizon_svf_comp_batch
+        dkw2, args2 = case(seed + 100)
+        d2 = synthetic.make_domain(**dkw2)
+        outs, st = horizon_svf_comp_batch([(d2.inputs(), args2), (d.inputs(), args)],
+                                          kernel=kernel, return_stats=True)
+        h, s = outs[1]
+        h2, s2 = outs[0]
+        ho2, so2, sto2 = oracle.horizon_svf(*d2.inputs(), *args2)
+        assert_parity(h2, s2, ho2, so2)
+        sto = dict(sto, num_rays=sto["num_rays"] + sto2["num_rays"])
+    else:
+        h, s, st = horizon_svf_comp_py(*d.inputs(), *args, kernel=kernel, return_stats=True)
     assert_parity(h, s, ho, so)
-    assert st["n_tri"] == sto["n_tri"]
+    if entry != 2:
+        assert st["n_tri"] == sto["n_tri"]
     assert abs(st["num_rays"] - sto["num_rays"]) <= 0.001 * sto["num_rays"]
