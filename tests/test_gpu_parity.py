@@ -371,3 +371,23 @@ def test_gpu_cell_ranges_at_the_ends(small_domain):
         hr, sr = horizon_svf_comp_py(*small_domain.inputs(), *args, cells=(b, e))
         np.testing.assert_array_equal(hr[:, b:e], h[:, b:e])
         np.testing.assert_array_equal(sr[b:e], s[b:e])
+
+
+def test_gpu_concurrent_calls_from_threads():
+    """Calls from several host threads at once (the library serialises them
+    per device) give the results of sequential calls."""
+    from concurrent.futures import ThreadPoolExecutor
+    doms = [synthetic.make_domain(edge_km=2.5, box_km=30.0 + 5 * k, seed=40 + k) for k in range(4)]
+    argsets = [(24, 1, 40000.0, 0.2, 1, 2), (16, 0, 20000.0, 0.5, 2, 1),
+               (36, 1, 30000.0, 0.2, 1, 0), (8, 1, 40000.0, 1.0, 3, 2)]
+    ref = [horizon_svf_comp_py(*d.inputs(), *a) for d, a in zip(doms, argsets)]
+
+    def run(k):
+        return [horizon_svf_comp_py(*doms[k].inputs(), *argsets[k]) for _ in range(3)]
+
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        outs = list(ex.map(run, range(4)))
+    for k in range(4):
+        for h, s in outs[k]:
+            np.testing.assert_array_equal(h, ref[k][0])
+            np.testing.assert_array_equal(s, ref[k][1])
