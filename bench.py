@@ -206,40 +206,16 @@ def cpu_sample_run(dom, target_ray_s: float):
             "wall_s": wall}
 
 
-def precision_report(dom, d_in, h_ref, s_ref, stream, sample=20000):
-    """Reference-frame vs local-frame arithmetic against the FP64 oracle."""
+def precision_report(d_in, h_ref, stream):
+    """The local-frame arithmetic (HZ_PRECISION_LOCAL) on the same workload:
+    its search time and its agreement with the reference-frame results. The
+    error of both against the FP64 oracle is reported by
+    tests/precision_report.py."""
     from horayzon_extpar_gb300 import _lib, horizon_svf_comp_device
-    from oracle import api as oracle
-    h_loc, s_loc, st = horizon_svf_comp_device(*d_in, *ARGS, stream=stream,
-                                               precision=_lib.HZ_PRECISION_LOCAL)
-    h_loc, s_loc = h_loc.cpu().numpy(), s_loc.cpu().numpy()
-    cells = np.sort(np.random.default_rng(7).choice(dom.ncell, min(sample, dom.ncell),
-                                                    replace=False))
-    h64, s64, _ = oracle.horizon_svf(*dom.inputs(), *ARGS, precision=1, cells=cells)
-
-    # Cells whose 40 km search reaches the domain edge (functions.py:58-97,
-    # verification.py:302-304) are reported separately.
-    from horayzon_extpar_gb300.border import distance_to_border
-    dist = distance_to_border(dom.clon, dom.clat, dom.vlon, dom.vlat, dom.cells_of_vertex)
-    inner = dist[cells] >= ARGS[2] * 1e-3
-
-    def stats(h, s):
-        dh = np.abs(h[:, cells] - h64[:, cells])
-        ds = np.abs(s[cells] - s64[cells])
-        return {"frac_evals_differing": float(np.mean(dh > 1e-9)),
-                "max_abs_deg": float(dh.max()), "mean_abs_deg": float(dh.mean()),
-                "max_abs_svf": float(ds.max()), "mean_abs_svf": float(ds.mean()),
-                "border_masked": {"cells": int(inner.sum()),
-                                  "frac_evals_differing": float(np.mean(dh[:, inner] > 1e-9)),
-                                  "max_abs_deg": float(dh[:, inner].max()),
-                                  "max_abs_svf": float(ds[inner].max())}}
-
-    d = np.abs(h_loc - h_ref)
-    return {"oracle": "FP64 vertices, rays and triangle test (oracle/hz_oracle.c)",
-            "sample_cells": int(cells.size),
-            "reference_frame_vs_fp64": stats(h_ref, s_ref),
-            "local_frame_vs_fp64": stats(h_loc, s_loc),
-            "local_vs_reference_frame": {"frac_within_0.25deg": float(np.mean(d <= 0.25)),
+    h_loc, _, st = horizon_svf_comp_device(*d_in, *ARGS, stream=stream,
+                                           precision=_lib.HZ_PRECISION_LOCAL)
+    d = np.abs(h_loc.cpu().numpy() - h_ref)
+    return {"local_vs_reference_frame": {"frac_within_0.25deg": float(np.mean(d <= 0.25)),
                                          "frac_identical": float(np.mean(d <= 1e-9))},
             "local_frame_trace_ms": st["ms_trace"]}
 
@@ -520,7 +496,7 @@ def run_gpu(args):
     extras = {}
     if not args.no_extras and rank == 0:
         extras["learned"] = learned_report(dom, d_in, hz, sv, stream, ms, args)
-        extras["precision"] = precision_report(dom, d_in, hz, sv, stream)
+        extras["precision"] = precision_report(d_in, hz, stream)
         extras["batched_domains"] = batch_report(args)
         extras["drop_in_numpy"] = drop_in_report(dom, min(args.steps, 3))
         extras["configs"] = configs_report(dom, d_in, stream)
