@@ -299,6 +299,9 @@ struct Engine {
   size_t cap = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};
+  static constexpr int kSide = 8;        // streams the per-domain builds of a batch spread over
+  cudaStream_t side[kSide] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[kSide] = {};
   unsigned long long* pinned = nullptr;  // readbacks and descriptor staging
   size_t pinned_words = 0;
   Staging* staging = nullptr;            // pageable caller buffers (host entries)
@@ -308,6 +311,11 @@ struct Engine {
     HZ_CUDA(cudaSetDevice(dev));
     HZ_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     for (auto& e : ev) HZ_CUDA(cudaEventCreate(&e));
+    for (int k = 0; k < kSide; k++) {
+      HZ_CUDA(cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking));
+      HZ_CUDA(cudaEventCreateWithFlags(&join_ev[k], cudaEventDisableTiming));
+    }
+    HZ_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
     HZ_CUDA(staging_create(&staging));
     return reserve_pinned(4096);
   }
@@ -351,6 +359,33 @@ struct Engine {
     if (arena) cudaFree(arena);
     arena = nullptr;
     cap = 0;
+  }
+};
+
+// The per-domain work of a loop spread over the engine's side streams
+// (domain d on side[d % k]) behind an event recorded on s; s then waits for
+// all of them. Inside a stream capture these become fork and join edges of
+// the graph. With one domain the work stays on s.
+struct Fork {
+  Engine& E;
+  cudaStream_t s;
+  int used;
+  Fork(Engine& e, cudaStream_t st, int n)
+      : E(e), s(st), used(n > 1 ? std::min(n, Engine::kSide) : 0) {}
+  cudaError_t begin() {
+    if (!used) return cudaSuccess;
+    cudaError_t e = cudaEventRecord(E.fork_ev, s);
+    for (int k = 0; k < used && e == cudaSuccess; k++) e = cudaStreamWaitEvent(E.side[k], E.fork_ev, 0);
+    return e;
+  }
+  cudaStream_t on(int d) const { return used ? E.side[d % used] : s; }
+  cudaError_t end() {
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < used && e == cudaSuccess; k++) {
+      e = cudaEventRecord(E.join_ev[k], E.side[k]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, E.join_ev[k], 0);
+    }
+    return e;
   }
 };
 
@@ -555,9 +590,14 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   if (stop == Stop::kEnu) return HZ_OK;
 
   // ---- BVH (cpp:395-432) ----
-  for (int d = 0; d < n; d++)
-    HZ_CUDA(bvh_build(b[d].vert32, b[d].vot, out->n_tri[d], b[d].nodes, b[d].tris, b[d].bvh, s,
-                      b[d].vert_lo, b[d].tri_lo, b[d].nodes4, opt.leaf_size));
+  {
+    Fork fk(E, s, n);
+    HZ_CUDA(fk.begin());
+    for (int d = 0; d < n; d++)
+      HZ_CUDA(bvh_build(b[d].vert32, b[d].vot, out->n_tri[d], b[d].nodes, b[d].tris, b[d].bvh,
+                        fk.on(d), b[d].vert_lo, b[d].tri_lo, b[d].nodes4, opt.leaf_size));
+    HZ_CUDA(fk.end());
+  }
   HZ_CUDA(cap.record(E.ev[2]));
   phase.next("hz: search");
 
@@ -648,11 +688,13 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       }
     }
     long long total = 0;
+    Fork fk(E, s, learned ? 1 : n);  // the learned start's kernels stay on s
+    HZ_CUDA(fk.begin());
     for (int d = 0; d < n; d++) {
       const Problem& P = pr[d];
       const int L = P.nhori * P.refine;
       HZ_CUDA(trace_tables(b[d].azim_cs, b[d].elev_cs, b[d].sin_lattice, L, shift[d],
-                           hori_acc, s));
+                           hori_acc, fk.on(d)));
       if (learned) {
         HZ_CUDA(raster_build(b[d].vert32, b[d].vot, out->n_tri[d], rdesc[d], b[d].rz_bits,
                              b[d].rz, s));
@@ -678,7 +720,8 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
         HZ_CUDA(learn_features(q, opt.mlp_params ? bb.mlp : nullptr, s));
       }
       HZ_CUDA(cell_order(b[d].cell_enu, P.cell_begin, P.cell_count, (int)(total - P.cell_begin),
-                         bb.order + total, b[d].order_scratch, b[d].cell_bounds, bb.work, s));
+                         bb.order + total, b[d].order_scratch, b[d].cell_bounds, bb.work,
+                         fk.on(d)));
       DomainDesc D;
       std::memset(&D, 0, sizeof(D));
       D.cell_enu = b[d].cell_enu;
@@ -718,6 +761,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       desc[d] = D;
       total += P.cell_count;
     }
+    HZ_CUDA(fk.end());
     if (total > INT32_MAX - (1ll << 26))
       return fail(HZ_ERR_VALUE, "more than 2^31 - 2^26 cells in one call");
     HZ_CUDA(cudaMemcpyAsync(bb.doms, desc, sizeof(DomainDesc) * (size_t)n,
