@@ -516,16 +516,22 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   // ---- mesh (cpp:228-317) ----
   unsigned long long* pin_tot = pin + 64;
   unsigned long long* pin_err = pin + 64 + n;
-  for (int d = 0; d < n; d++) {
-    const Problem& P = pr[d];
-    HZ_CUDA(mesh_count(P.cov, P.nvert, P.ncell, P.grid_type, b[d].packed, b[d].err, s));
-    if (P.nvert > 0) {
-      HZ_CUDA(scan_exclusive_u64(b[d].packed, b[d].offsets, P.nvert, b[d].totals,
-                                 b[d].scan_partials, s));
-      HZ_CUDA(cudaMemcpyAsync(pin_tot + d, b[d].totals, sizeof(unsigned long long),
-                              cudaMemcpyDeviceToHost, s));
+  {
+    Fork fk(E, s, n);
+    HZ_CUDA(fk.begin());
+    for (int d = 0; d < n; d++) {
+      const Problem& P = pr[d];
+      const cudaStream_t sd = fk.on(d);
+      HZ_CUDA(mesh_count(P.cov, P.nvert, P.ncell, P.grid_type, b[d].packed, b[d].err, sd));
+      if (P.nvert > 0) {
+        HZ_CUDA(scan_exclusive_u64(b[d].packed, b[d].offsets, P.nvert, b[d].totals,
+                                   b[d].scan_partials, sd));
+        HZ_CUDA(cudaMemcpyAsync(pin_tot + d, b[d].totals, sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, sd));
+      }
+      HZ_CUDA(cudaMemcpyAsync(pin_err + d, b[d].err, sizeof(int), cudaMemcpyDeviceToHost, sd));
     }
-    HZ_CUDA(cudaMemcpyAsync(pin_err + d, b[d].err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    HZ_CUDA(fk.end());
   }
   HZ_CUDA(cudaStreamSynchronize(s));
   std::vector<int> nadd(n);
@@ -541,24 +547,34 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       return fail(HZ_ERR_VALUE, "mesh of %d triangles exceeds 2^27 per domain", out->n_tri[d]);
     out->n_mv[d] = pr[d].ncell + nadd[d];
   }
-  for (int d = 0; d < n; d++) {
-    const Problem& P = pr[d];
-    HZ_CUDA(mesh_emit(P.clon, P.clat, P.hsurf, P.vlon, P.vlat, P.cov, P.nvert, P.ncell,
-                      P.grid_type, b[d].offsets, b[d].vot, b[d].add_lon, b[d].add_lat,
-                      b[d].add_h, s));
+  {
+    Fork fk(E, s, n);
+    HZ_CUDA(fk.begin());
+    for (int d = 0; d < n; d++) {
+      const Problem& P = pr[d];
+      HZ_CUDA(mesh_emit(P.clon, P.clat, P.hsurf, P.vlon, P.vlat, P.cov, P.nvert, P.ncell,
+                        P.grid_type, b[d].offsets, b[d].vot, b[d].add_lon, b[d].add_lat,
+                        b[d].add_h, fk.on(d)));
+    }
+    HZ_CUDA(fk.end());
   }
   if (stop == Stop::kMesh) return HZ_OK;
 
   // ---- frames (cpp:611-644) ----
-  for (int d = 0; d < n; d++) {
-    const Problem& P = pr[d];
-    HZ_CUDA(mesh_ecef(P.clon, P.clat, P.hsurf, b[d].add_lon, b[d].add_lat, b[d].add_h,
-                      P.ncell, nadd[d], b[d].ecef, b[d].block_sums, b[d].origin_sum, s));
-  }
   double* sums = reinterpret_cast<double*>(pin + 64 + 2 * n);
-  for (int d = 0; d < n; d++)
-    HZ_CUDA(cudaMemcpyAsync(sums + 3 * d, b[d].origin_sum, 3 * sizeof(double),
-                            cudaMemcpyDeviceToHost, s));
+  {
+    Fork fk(E, s, n);
+    HZ_CUDA(fk.begin());
+    for (int d = 0; d < n; d++) {
+      const Problem& P = pr[d];
+      HZ_CUDA(mesh_ecef(P.clon, P.clat, P.hsurf, b[d].add_lon, b[d].add_lat, b[d].add_h,
+                        P.ncell, nadd[d], b[d].ecef, b[d].block_sums, b[d].origin_sum,
+                        fk.on(d)));
+      HZ_CUDA(cudaMemcpyAsync(sums + 3 * d, b[d].origin_sum, 3 * sizeof(double),
+                              cudaMemcpyDeviceToHost, fk.on(d)));
+    }
+    HZ_CUDA(fk.end());
+  }
   HZ_CUDA(cudaStreamSynchronize(s));
   std::vector<Frame> frames(n);
   for (int d = 0; d < n; d++) {
@@ -582,9 +598,14 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   HZ_CUDA(cap.begin());
   const cudaStream_t s_call = s;
   if (cap.capturing) s = cap.s;
-  for (int d = 0; d < n; d++)
-    HZ_CUDA(mesh_enu(b[d].ecef, out->n_mv[d], pr[d].ncell, frames[d], b[d].vert32,
-                     b[d].cell_enu, b[d].vert_lo, s));
+  {
+    Fork fk(E, s, n);
+    HZ_CUDA(fk.begin());
+    for (int d = 0; d < n; d++)
+      HZ_CUDA(mesh_enu(b[d].ecef, out->n_mv[d], pr[d].ncell, frames[d], b[d].vert32,
+                       b[d].cell_enu, b[d].vert_lo, fk.on(d)));
+    HZ_CUDA(fk.end());
+  }
   HZ_CUDA(cap.record(E.ev[1]));
   phase.next("hz: bvh");
   if (stop == Stop::kEnu) return HZ_OK;
