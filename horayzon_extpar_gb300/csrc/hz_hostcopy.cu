@@ -47,6 +47,10 @@ struct Staging {
   unsigned long long generation = 0;
   int pending = 0;
   bool stop = false;
+  // Upload ring: the chunk the next upload piece uses, and whether a chunk's
+  // last device copy may still be reading it (its `done` event is pending).
+  int next = 0;
+  bool in_flight[2] = {false, false};
 
   ~Staging() {
     {
@@ -137,6 +141,15 @@ cudaError_t copy_to_host(Staging* st, void* dst, const void* src_dev, size_t byt
     return cudaMemcpyAsync(dst, src_dev, bytes, cudaMemcpyDeviceToHost, s);
   const char* src = static_cast<const char*>(src_dev);
   char* out = static_cast<char*>(dst);
+  // Uploads still reading a chunk finish first (they may be on another
+  // stream); afterwards the chunks are free.
+  for (int k = 0; k < 2; k++) {
+    if (st->in_flight[k]) {
+      const cudaError_t e = cudaEventSynchronize(st->done[k]);
+      if (e != cudaSuccess) return e;
+      st->in_flight[k] = false;
+    }
+  }
   const size_t n = (bytes + kChunkBytes - 1) / kChunkBytes;
   for (size_t i = 0; i <= n; i++) {
     if (i < n) {  // device -> chunk i % 2 (that chunk's previous contents are copied out)
@@ -162,22 +175,23 @@ cudaError_t copy_from_host(Staging* st, void* dst_dev, const void* src, size_t b
     return cudaMemcpyAsync(dst_dev, src, bytes, cudaMemcpyHostToDevice, s);
   const char* in = static_cast<const char*>(src);
   char* dst = static_cast<char*>(dst_dev);
-  const size_t n = (bytes + kChunkBytes - 1) / kChunkBytes;
-  for (size_t i = 0; i < n; i++) {
-    const size_t off = i * kChunkBytes, len = std::min(kChunkBytes, bytes - off);
-    if (i >= 2) {  // the chunk's previous upload must have left it
-      const cudaError_t e = cudaEventSynchronize(st->done[i % 2]);
+  // Pieces go through the two chunks in turn, across calls: a chunk is
+  // refilled only after its previous device copy has left it, so the host
+  // copy of one piece overlaps the device copy of the one before. The
+  // caller's buffer is no longer needed when this returns.
+  for (size_t off = 0; off < bytes; off += kChunkBytes) {
+    const size_t len = std::min(kChunkBytes, bytes - off);
+    const int k = st->next;
+    if (st->in_flight[k]) {
+      const cudaError_t e = cudaEventSynchronize(st->done[k]);
       if (e != cudaSuccess) return e;
     }
-    st->parallel_copy(st->chunk[i % 2], in + off, len);
-    cudaError_t e = cudaMemcpyAsync(dst + off, st->chunk[i % 2], len, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaEventRecord(st->done[i % 2], s);
+    st->parallel_copy(st->chunk[k], in + off, len);
+    cudaError_t e = cudaMemcpyAsync(dst + off, st->chunk[k], len, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaEventRecord(st->done[k], s);
     if (e != cudaSuccess) return e;
-  }
-  // The chunks are reused by the next call: wait for the last uploads.
-  for (int k = 0; k < 2; k++) {
-    const cudaError_t e = cudaEventSynchronize(st->done[k]);
-    if (e != cudaSuccess) return e;
+    st->in_flight[k] = true;
+    st->next = k ^ 1;
   }
   return cudaSuccess;
 }
