@@ -110,3 +110,18 @@ def test_learned_start_keeps_results_and_saves_rays(trained):
     assert r["learned"] < r["plain"]
     assert r["learned"] < r["untrained"]
     assert r["every"] >= 2.0 - 1e-9  # a bracket always needs a hit and a miss
+
+
+def test_learned_start_in_a_batch_equals_single_calls(trained):
+    """Each domain of a batch gets its own raster and features: the learned
+    start gives every domain the results of its own call."""
+    from horayzon_extpar_gb300.horizon_svf import horizon_svf_comp_batch
+    p, kw, args = trained
+    doms = [synthetic.make_domain(seed=s, **kw) for s in (8, 9)]
+    args2 = (16, 1, 6000.0, 0.2, 2, 1)
+    outs = horizon_svf_comp_batch([(doms[0].inputs(), args), (doms[1].inputs(), args2)],
+                                  mlp_params=p)
+    for d, a, (h, s) in zip(doms, (args, args2), outs):
+        h1, s1 = horizon_svf_comp_py(*d.inputs(), *a, mlp_params=p)
+        np.testing.assert_array_equal(h, h1)
+        np.testing.assert_array_equal(s, s1)
