@@ -136,7 +136,7 @@ struct Buffers {
   void* order_scratch;
   unsigned* cell_bounds;
   double2 *azim_cs, *elev_cs;
-  double* sin_lattice;
+  double* svf_lattice;
   int* err;
 };
 
@@ -207,7 +207,7 @@ Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhor
   b.cell_bounds = c.take<unsigned>(8);
   b.azim_cs = c.take<double2>(nhori * 50);  // L <= num_hori * max refine_factor
   b.elev_cs = c.take<double2>(kElevTable);
-  b.sin_lattice = c.take<double>(kSinTable);
+  b.svf_lattice = c.take<double>(kSvfTable);
   b.err = c.take<int>(4);
   return b;
 }
@@ -714,8 +714,8 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     for (int d = 0; d < n; d++) {
       const Problem& P = pr[d];
       const int L = P.nhori * P.refine;
-      HZ_CUDA(trace_tables(b[d].azim_cs, b[d].elev_cs, b[d].sin_lattice, L, shift[d],
-                           hori_acc, fk.on(d)));
+      HZ_CUDA(trace_tables(b[d].azim_cs, b[d].elev_cs, b[d].svf_lattice, L, shift[d],
+                           hori_acc, P.svf_type, fk.on(d)));
       if (learned) {
         HZ_CUDA(raster_build(b[d].vert32, b[d].vot, out->n_tri[d], rdesc[d], b[d].rz_bits,
                              b[d].rz, s));
@@ -758,7 +758,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.skyview = P.skyview;
       D.azim_cs = b[d].azim_cs;
       D.elev_cs = b[d].elev_cs;
-      D.sin_lattice = b[d].sin_lattice;
+      D.svf_lattice = b[d].svf_lattice;
       D.done = n > 1 ? bb.done + 2 * d : nullptr;
       D.start_m = opt.mlp_params ? b[d].start_m : nullptr;
       D.start_all = opt.mlp_every_azimuth ? 1 : 0;

@@ -16,6 +16,7 @@ namespace hz {
 
 constexpr double kEarthRadius = 6371229.0;  // mo_lradtopo_horayzon.cpp:584
 constexpr double kPi = 3.14159265358979323846;
+constexpr double kInvPi = 1.0 / kPi;       // RN(1 / kPi) = 0x1.45f306dc9c883p-2
 constexpr int kLeafMax = 2;                 // default triangles per BVH leaf (<= 8)
 constexpr int kStackDepth = 64;             // >= LBVH depth (32 key + 32 index bits)
 constexpr int kEmptyRef = INT32_MIN;        // no child / empty tree

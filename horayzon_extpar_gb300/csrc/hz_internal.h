@@ -97,20 +97,20 @@ struct TraceParams {
   double* skyview;          // [ncell]
   unsigned long long* counters;  // [0] rays, [1] node visits, [2] triangle tests
   int* err;
-  // Lattice tables of the persistent search (trace_tables):
-  const double2* azim_cs;   // [L] cos, sin of azimuth shift + a * 360 deg / L
-  const double2* elev_cs;   // [kElevTable] cos, sin of m * 0.5 deg, m = kElevMin + i
-  const double* sin_lattice;  // [kSinTable] sin(j * 0.25 deg)
 };
 
+// Lattice tables of the persistent search (trace_tables): azim_cs [L] cos,
+// sin of azimuth shift + a * 360 deg / L; elev_cs [kElevTable] cos, sin of
+// m * 0.5 deg, m = kElevMin + i; svf_lattice [kSvfTable] the SVF term
+// 1 - sin(j * 0.25 deg)^(svf_type + 1) of a clipped horizon on the lattice.
 constexpr int kElevMin = -256;
 constexpr int kElevTable = 1280;
-constexpr int kSinTable = 2560;
+constexpr int kSvfTable = 2560;
 
-// Fills the lattice tables of p (device FP64 sin/cos), L = p.L entries of
-// azim_cs; shift is the reference's azimuth shift (cpp:662-668).
-cudaError_t trace_tables(double2* azim_cs, double2* elev_cs, double* sin_lattice, int L,
-                         double shift, double hori_acc, cudaStream_t s);
+// Fills the lattice tables (device FP64 sin/cos); shift is the reference's
+// azimuth shift (cpp:662-668).
+cudaError_t trace_tables(double2* azim_cs, double2* elev_cs, double* svf_lattice, int L,
+                         double shift, double hori_acc, int svf_type, cudaStream_t s);
 // One thread per cell, nested loops as in the reference (simple; kept as the
 // second implementation the flattened kernel is tested against).
 // Any-hit flags (hit[i] = 1) of n_ray rays (org, dir: float3 on the device)
@@ -147,7 +147,7 @@ struct DomainDesc {
   double* skyview;            // [ncell] (the search leaves the sums over azimuths)
   const double2* azim_cs;     // lattice tables (trace_tables)
   const double2* elev_cs;
-  const double* sin_lattice;
+  const double* svf_lattice;
   unsigned long long* done;   // optional: [0] finished cells, [1] globaltimer at the last
   const int16_t* start_m;     // optional learned start lattice index [L][ncell]
   int start_all;              // 1: learned start at every azimuth; 0: azimuth 0 only

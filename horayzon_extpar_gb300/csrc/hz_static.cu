@@ -81,7 +81,7 @@ struct StaticBuffers {
   unsigned* cell_bounds;
   int* work;
   double2 *azim_cs, *elev_cs;
-  double* sin_lattice;
+  double* svf_lattice;
   DomainDesc* dom;
   unsigned long long* counters;
   int* err;
@@ -126,7 +126,7 @@ StaticBuffers lay_out(Layout& L, long long ncell, long long nvert, long long max
   b.work = L.take<int>(4);
   b.azim_cs = L.take<double2>(num_azimuths);
   b.elev_cs = L.take<double2>(kElevTable);
-  b.sin_lattice = L.take<double>(kSinTable);
+  b.svf_lattice = L.take<double>(kSvfTable);
   b.dom = L.take<DomainDesc>(1);
   b.counters = L.take<unsigned long long>(kCounterWords);
   b.err = L.take<int>(4);
@@ -276,7 +276,7 @@ extern "C" int hz_horizon_svf_device_static(
   D.skyview = skyview;
   D.azim_cs = b.azim_cs;
   D.elev_cs = b.elev_cs;
-  D.sin_lattice = b.sin_lattice;
+  D.svf_lattice = b.svf_lattice;
   D.centre = fr.centre;
   D.pole = fr.pole;
   D.ray_org_elev = ray_org_elev;
@@ -298,8 +298,8 @@ extern "C" int hz_horizon_svf_device_static(
                  "search descriptor");
   HZ_STATIC_CUDA(cell_order(b.cell_enu, 0, num_cell, 0, b.order, b.order_scratch, b.cell_bounds,
                             b.work, s), "cell order");
-  HZ_STATIC_CUDA(trace_tables(b.azim_cs, b.elev_cs, b.sin_lattice, L, azim_shift, D.hori_acc,
-                              s), "lattice tables");
+  HZ_STATIC_CUDA(trace_tables(b.azim_cs, b.elev_cs, b.svf_lattice, L, azim_shift, D.hori_acc,
+                              D.svf_type, s), "lattice tables");
   const TraceKnobs knobs{kDefaultAdvanceMin, kDefaultLeafMin, kDefaultChunk, kTraceBinary};
   HZ_STATIC_CUDA(trace_flat(b.dom, 1, b.order, num_cell, b.work, b.counters, b.err, knobs,
                             false, false, s), "horizon search");

@@ -553,6 +553,28 @@ __device__ __forceinline__ double svf_term(double s, int svf_type) {
   return 1.0 - (s * s * s);
 }
 
+// SVF term of a clipped horizon h ~ j * hori_acc: 1 for h = 0 (sin 0 = 0),
+// the tabulated term of the lattice value, or computed off the table.
+__device__ __forceinline__ double lattice_svf_term(const DomainDesc& D, double h, int j) {
+  if (!(h > 0.0)) return 1.0;
+  if (j > 0 && j < kSvfTable) return __ldg(&D.svf_lattice[j]);
+  return svf_term(sin(h), D.svf_type);
+}
+
+// RN(v / pi) without a division, by Markstein's correction for a divisor
+// known in advance (P. Markstein, "Computation of elementary functions on the
+// IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990): y =
+// RN(1 / pi) lies within 0.131 ulp of 1 / pi, so for a normal v >= 0
+// q0 = RN(v * y) is within 0.206 + 0.5 ulp of v / pi, a faithful quotient;
+// its remainder r = v - q0 * pi is then exact in one FMA, and RN(q0 + r * y)
+// is the correctly rounded quotient, the value of v / pi. The search's sums
+// are 0 or at least 0.25 deg, far from the subnormal range.
+__device__ __forceinline__ double div_pi_rn(double v) {
+  const double q0 = __dmul_rn(v, kInvPi);
+  const double r = __fma_rn(-q0, kPi, v);
+  return __fma_rn(r, kInvPi, q0);
+}
+
 // Domain of work id g (doms sorted by cell_offset).
 __device__ __forceinline__ int domain_of(const DomainDesc* __restrict__ doms, int ndom,
                                          long long g) {
@@ -659,11 +681,7 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       // holds every clipped h, and k_finish_outputs sums the SVF from it in
       // the same order.
       double svf = SV(8);
-      if (D.refine != 1) {
-        double s = 0.0;
-        if (h > 0.0) s = (j > 0 && j < kSinTable) ? __ldg(&D.sin_lattice[j]) : sin(h);
-        svf = svf + svf_term(s, D.svf_type);
-      }
+      if (D.refine != 1) svf = svf + lattice_svf_term(D, h, j);
       a++;
       if (a == D.L) {
         if (D.refine != 1) D.skyview[cell] = svf;  // divided by L in k_finish_outputs
@@ -1050,11 +1068,15 @@ __global__ void k_cell_frames(const DomainDesc* __restrict__ doms, int ndom,
 }
 
 // The search's sums to outputs (cpp:736-754): horizon sector sums [rad] ->
-// degrees and mean over refine_factor; SVF sum -> mean over the azimuths.
-// x / 1.0 == x exactly, so that division is skipped for refine_factor 1.
-// One thread per traced cell in index order (coalesced rows of horizon):
-// thread k is the (k - k_begin)-th traced cell of the domain holding
-// position k.
+// degrees (v / pi * 180, the division by div_pi_rn) and mean over
+// refine_factor; SVF sum -> mean over the azimuths. x / 1.0 == x exactly, so
+// that division is skipped for refine_factor 1. One thread per traced cell
+// in index order (coalesced rows of horizon): thread k is the
+// (k - k_begin)-th traced cell of the domain holding position k. A thread
+// reads kFinishRows rows before it converts and stores them, so that several
+// loads are in flight per thread.
+constexpr int kFinishRows = 8;
+
 __global__ void k_finish_outputs(const DomainDesc* __restrict__ doms, int ndom, int total) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= total) return;
@@ -1066,24 +1088,28 @@ __global__ void k_finish_outputs(const DomainDesc* __restrict__ doms, int ndom, 
   }
   const DomainDesc& D = doms[lo];
   const int cell = D.cell_begin + (int)(k - D.k_begin);
-  const bool svf_here = D.refine == 1;
+  const long long nc = D.ncell;
+  const int nhori = D.nhori;
+  const int refine = D.refine;
+  const bool svf_here = refine == 1;
   const double inv_ha = 1.0 / D.hori_acc;
+  double* col = D.horizon + cell;
   double svf = 0.0;
-  for (int j = 0; j < D.nhori; j++) {
-    double* h = D.horizon + (long long)j * D.ncell + cell;
-    const double v = *h;
-    if (svf_here) {
-      // v is the clipped h of azimuth j; h > 0 lies on the lattice j_lat *
-      // hori_acc up to the rounding of the elevation sum, which recovers j_lat.
-      double s = 0.0;
-      if (v > 0.0) {
-        const int jl = (int)rint(v * inv_ha);
-        s = (jl > 0 && jl < kSinTable) ? __ldg(&D.sin_lattice[jl]) : sin(v);
-      }
-      svf = svf + svf_term(s, D.svf_type);
+  for (int j0 = 0; j0 < nhori; j0 += kFinishRows) {
+    double v[kFinishRows];
+#pragma unroll
+    for (int u = 0; u < kFinishRows; u++)
+      v[u] = j0 + u < nhori ? col[(long long)(j0 + u) * nc] : 0.0;
+#pragma unroll
+    for (int u = 0; u < kFinishRows; u++) {
+      if (j0 + u >= nhori) break;
+      // v is the clipped h of azimuth j0 + u when svf_here; h > 0 lies on
+      // the lattice j * hori_acc up to the rounding of the elevation sum,
+      // which recovers j.
+      if (svf_here) svf = svf + lattice_svf_term(D, v[u], __double2int_rn(v[u] * inv_ha));
+      const double deg = __dmul_rn(div_pi_rn(v[u]), 180.0);
+      col[(long long)(j0 + u) * nc] = refine == 1 ? deg : deg / (double)refine;
     }
-    const double deg = (v / kPi) * 180.0;
-    *h = D.refine == 1 ? deg : deg / (double)D.refine;
   }
   D.skyview[cell] = (svf_here ? svf : D.skyview[cell]) / (double)D.L;
 }
@@ -1165,11 +1191,11 @@ __global__ void k_cell_keys(const double* __restrict__ cell_enu, int begin, int 
 }
 
 // Lattice tables: azimuths theta_a = shift + a * 2 pi / L (cpp:653-668),
-// elevations m * 2 * hori_acc (cpp:527, 538) and sin(j * hori_acc) for the
-// SVF of clipped horizons on the lattice.
+// elevations m * 2 * hori_acc (cpp:527, 538) and the SVF term of
+// sin(j * hori_acc) for clipped horizons on the lattice (cpp:333-358).
 __global__ void k_trace_tables(double2* __restrict__ azim_cs, double2* __restrict__ elev_cs,
-                               double* __restrict__ sin_lattice, int L, double shift,
-                               double hori_acc) {
+                               double* __restrict__ svf_lattice, int L, double shift,
+                               double hori_acc, int svf_type) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < L) {
     const double th = shift + (double)i * ((2.0 * kPi) / (double)L);
@@ -1179,7 +1205,7 @@ __global__ void k_trace_tables(double2* __restrict__ azim_cs, double2* __restric
     const double e = (double)(kElevMin + i) * (2.0 * hori_acc);
     elev_cs[i] = make_double2(cos(e), sin(e));
   }
-  if (i < kSinTable) sin_lattice[i] = sin((double)i * hori_acc);
+  if (i < kSvfTable) svf_lattice[i] = svf_term(sin((double)i * hori_acc), svf_type);
 }
 
 __global__ void k_init_cell_bounds(unsigned* b, int* work) {
@@ -1192,11 +1218,11 @@ __global__ void k_init_cell_bounds(unsigned* b, int* work) {
 
 }  // namespace
 
-cudaError_t trace_tables(double2* azim_cs, double2* elev_cs, double* sin_lattice, int L,
-                         double shift, double hori_acc, cudaStream_t s) {
-  const int n = L > kSinTable ? L : kSinTable;
-  k_trace_tables<<<grid_for(n, 256), 256, 0, s>>>(azim_cs, elev_cs, sin_lattice, L, shift,
-                                                  hori_acc);
+cudaError_t trace_tables(double2* azim_cs, double2* elev_cs, double* svf_lattice, int L,
+                         double shift, double hori_acc, int svf_type, cudaStream_t s) {
+  const int n = L > kSvfTable ? L : kSvfTable;
+  k_trace_tables<<<grid_for(n, 256), 256, 0, s>>>(azim_cs, elev_cs, svf_lattice, L, shift,
+                                                  hori_acc, svf_type);
   note_launches(1);
   return cudaGetLastError();
 }

@@ -25,6 +25,10 @@ def assert_parity(h, s, h_ref, s_ref, min_exact=0.999):
         d <= HORIZON_TOL_DEG)
     assert np.mean(d <= EXACT_DEG) >= min_exact, "exact fraction %.6f" % np.mean(
         d <= EXACT_DEG)
+    # Where the searches agree the degrees agree bit for bit (the same sums,
+    # and the epilogue's division-free rad -> deg is the IEEE quotient).
+    same = d <= EXACT_DEG
+    np.testing.assert_array_equal(h[same], h_ref[same])
     assert np.abs(s - s_ref).max() <= SVF_TOL
 
 
