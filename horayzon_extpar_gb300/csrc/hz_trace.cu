@@ -575,6 +575,23 @@ __device__ __forceinline__ double div_pi_rn(double v) {
   return __fma_rn(r, kInvPi, q0);
 }
 
+// The epilogue's SVF term of a clipped horizon v (0, or at least 0.25 deg on
+// the lattice v ~ j * hori_acc, j < kSvfTable in practice), with integer and
+// FP32 operations where the search's form uses FP64 ones: v > 0 from the
+// exponent bits, and j from an FP32 copy of v truncated to its top 20
+// mantissa bits (relative error < 2^-20, so |f / hori_acc - j| < 0.01).
+__device__ __forceinline__ double finish_svf_term(const DomainDesc& D, double v, float inv_ha) {
+  const int hi = __double2hiint(v);
+  const int e = (hi >> 20) & 0x7ff;
+  if (hi < 0 || e == 0) return 1.0;  // v == 0 (the clip leaves no negatives)
+  const int fe = e - 1023 + 127;
+  if (fe <= 0 || fe >= 255) return svf_term(sin(v), D.svf_type);
+  const float f = __int_as_float((fe << 23) | ((hi & 0xfffff) << 3));
+  const int j = __float2int_rn(f * inv_ha);
+  if (j > 0 && j < kSvfTable) return __ldg(&D.svf_lattice[j]);
+  return svf_term(sin(v), D.svf_type);
+}
+
 // Domain of work id g (doms sorted by cell_offset).
 __device__ __forceinline__ int domain_of(const DomainDesc* __restrict__ doms, int ndom,
                                          long long g) {
@@ -1092,7 +1109,7 @@ __global__ void k_finish_outputs(const DomainDesc* __restrict__ doms, int ndom, 
   const int nhori = D.nhori;
   const int refine = D.refine;
   const bool svf_here = refine == 1;
-  const double inv_ha = 1.0 / D.hori_acc;
+  const float inv_ha = (float)(1.0 / D.hori_acc);
   double* col = D.horizon + cell;
   double svf = 0.0;
   for (int j0 = 0; j0 < nhori; j0 += kFinishRows) {
@@ -1104,9 +1121,8 @@ __global__ void k_finish_outputs(const DomainDesc* __restrict__ doms, int ndom, 
     for (int u = 0; u < kFinishRows; u++) {
       if (j0 + u >= nhori) break;
       // v is the clipped h of azimuth j0 + u when svf_here; h > 0 lies on
-      // the lattice j * hori_acc up to the rounding of the elevation sum,
-      // which recovers j.
-      if (svf_here) svf = svf + lattice_svf_term(D, v[u], __double2int_rn(v[u] * inv_ha));
+      // the lattice j * hori_acc up to the rounding of the elevation sum.
+      if (svf_here) svf = svf + finish_svf_term(D, v[u], inv_ha);
       const double deg = __dmul_rn(div_pi_rn(v[u]), 180.0);
       col[(long long)(j0 + u) * nc] = refine == 1 ? deg : deg / (double)refine;
     }
