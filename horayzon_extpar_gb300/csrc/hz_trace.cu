@@ -1087,12 +1087,43 @@ __global__ void k_cell_frames(const DomainDesc* __restrict__ doms, int ndom,
 // The search's sums to outputs (cpp:736-754): horizon sector sums [rad] ->
 // degrees (v / pi * 180, the division by div_pi_rn) and mean over
 // refine_factor; SVF sum -> mean over the azimuths. x / 1.0 == x exactly, so
-// that division is skipped for refine_factor 1. One thread per traced cell
-// in index order (coalesced rows of horizon): thread k is the
-// (k - k_begin)-th traced cell of the domain holding position k. A thread
-// reads kFinishRows rows before it converts and stores them, so that several
-// loads are in flight per thread.
+// that division is left out for refine_factor 1 (kRefine1: a separate
+// instance, so that no division is evaluated and discarded per value). One
+// thread per traced cell in index order (coalesced rows of horizon): thread
+// k is the (k - k_begin)-th traced cell of the domain holding position k. A
+// thread reads kFinishRows rows before it converts and stores them, so that
+// several loads are in flight per thread.
 constexpr int kFinishRows = 8;
+
+template <bool kRefine1>
+__device__ __forceinline__ void finish_cell(const DomainDesc& D, int cell) {
+  const long long nc = D.ncell;
+  const int nhori = D.nhori;
+  const double refine = (double)D.refine;
+  const float inv_ha = (float)(1.0 / D.hori_acc);
+  double* col = D.horizon + cell;
+  double svf = 0.0;
+  for (int j0 = 0; j0 < nhori; j0 += kFinishRows) {
+    double v[kFinishRows];
+#pragma unroll
+    for (int u = 0; u < kFinishRows; u++)
+      v[u] = j0 + u < nhori ? col[(long long)(j0 + u) * nc] : 0.0;
+#pragma unroll
+    for (int u = 0; u < kFinishRows; u++) {
+      if (j0 + u >= nhori) break;
+      const double deg = __dmul_rn(div_pi_rn(v[u]), 180.0);
+      if (kRefine1) {
+        // v is the clipped h of azimuth j0 + u; h > 0 lies on the lattice
+        // j * hori_acc up to the rounding of the elevation sum.
+        svf = svf + finish_svf_term(D, v[u], inv_ha);
+        col[(long long)(j0 + u) * nc] = deg;
+      } else {
+        col[(long long)(j0 + u) * nc] = deg / refine;
+      }
+    }
+  }
+  D.skyview[cell] = (kRefine1 ? svf : D.skyview[cell]) / (double)D.L;
+}
 
 __global__ void k_finish_outputs(const DomainDesc* __restrict__ doms, int ndom, int total) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1105,29 +1136,8 @@ __global__ void k_finish_outputs(const DomainDesc* __restrict__ doms, int ndom, 
   }
   const DomainDesc& D = doms[lo];
   const int cell = D.cell_begin + (int)(k - D.k_begin);
-  const long long nc = D.ncell;
-  const int nhori = D.nhori;
-  const int refine = D.refine;
-  const bool svf_here = refine == 1;
-  const float inv_ha = (float)(1.0 / D.hori_acc);
-  double* col = D.horizon + cell;
-  double svf = 0.0;
-  for (int j0 = 0; j0 < nhori; j0 += kFinishRows) {
-    double v[kFinishRows];
-#pragma unroll
-    for (int u = 0; u < kFinishRows; u++)
-      v[u] = j0 + u < nhori ? col[(long long)(j0 + u) * nc] : 0.0;
-#pragma unroll
-    for (int u = 0; u < kFinishRows; u++) {
-      if (j0 + u >= nhori) break;
-      // v is the clipped h of azimuth j0 + u when svf_here; h > 0 lies on
-      // the lattice j * hori_acc up to the rounding of the elevation sum.
-      if (svf_here) svf = svf + finish_svf_term(D, v[u], inv_ha);
-      const double deg = __dmul_rn(div_pi_rn(v[u]), 180.0);
-      col[(long long)(j0 + u) * nc] = refine == 1 ? deg : deg / (double)refine;
-    }
-  }
-  D.skyview[cell] = (svf_here ? svf : D.skyview[cell]) / (double)D.L;
+  if (D.refine == 1) finish_cell<true>(D, cell);
+  else finish_cell<false>(D, cell);
 }
 
 // Bounds of the traced cells' horizontal ENU positions (for their curve keys).
