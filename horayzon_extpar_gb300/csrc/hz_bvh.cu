@@ -60,22 +60,10 @@ __global__ void k_tri_bounds(const float* __restrict__ vert, const int* __restri
               fmaxf(fmaxf(fabsf(b.y), fabsf(b.z)),
                     fmaxf(fmaxf(fabsf(c.x), fabsf(c.y)), fabsf(c.z))));
   }
-  // Warp-level reduction, then one atomic per warp.
-  unsigned mnx = valid ? f2ord(cx) : 0xFFFFFFFFu, mny = valid ? f2ord(cy) : 0xFFFFFFFFu;
-  unsigned mxx = valid ? f2ord(cx) : 0u, mxy = valid ? f2ord(cy) : 0u;
-  unsigned mm = valid ? f2ord(m) : 0u;
-  mnx = __reduce_min_sync(0xffffffffu, mnx);
-  mny = __reduce_min_sync(0xffffffffu, mny);
-  mxx = __reduce_max_sync(0xffffffffu, mxx);
-  mxy = __reduce_max_sync(0xffffffffu, mxy);
-  mm = __reduce_max_sync(0xffffffffu, mm);
-  if ((threadIdx.x & 31) == 0) {
-    atomicMin(&bounds[0], mnx);
-    atomicMin(&bounds[1], mny);
-    atomicMax(&bounds[2], mxx);
-    atomicMax(&bounds[3], mxy);
-    atomicMax(&bounds[4], mm);
-  }
+  // Block-level reduction, then one atomic per value and block.
+  unsigned b[5] = {valid ? f2ord(cx) : 0xFFFFFFFFu, valid ? f2ord(cy) : 0xFFFFFFFFu,
+                   valid ? f2ord(cx) : 0u, valid ? f2ord(cy) : 0u, valid ? f2ord(m) : 0u};
+  block_bounds_atomic<2, 3>(b, bounds);
 }
 
 __global__ void k_morton(const float2* __restrict__ cxy, int n,

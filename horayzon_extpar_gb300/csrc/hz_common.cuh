@@ -84,6 +84,36 @@ __device__ __forceinline__ unsigned f2ord(float f) {
 __device__ __forceinline__ float ord2f(unsigned u) {
   return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
 }
+// Block-wide bounds of ordered keys: v[0 .. kMin) reduced by min, v[kMin ..
+// kMin + kMax) by max, over the whole block (blockDim.x a multiple of 32, at
+// most 1024; every thread of the block calls it), then one atomicMin /
+// atomicMax per value and block into out[]. Per-warp atomics on the same few
+// addresses serialise at L2; per block there are 8 (or 32) times fewer.
+template <int kMin, int kMax>
+__device__ __forceinline__ void block_bounds_atomic(unsigned (&v)[kMin + kMax],
+                                                    unsigned* out) {
+  constexpr int kN = kMin + kMax;
+  __shared__ unsigned part[kN][32];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int i = 0; i < kN; i++) {
+    v[i] = i < kMin ? __reduce_min_sync(0xffffffffu, v[i]) : __reduce_max_sync(0xffffffffu, v[i]);
+    if (l == 0) part[i][w] = v[i];
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int i = 0; i < kN; i++) {
+      unsigned x = l < nw ? part[i][l] : (i < kMin ? 0xFFFFFFFFu : 0u);
+      x = i < kMin ? __reduce_min_sync(0xffffffffu, x) : __reduce_max_sync(0xffffffffu, x);
+      if (l == 0) {
+        if (i < kMin) atomicMin(out + i, x);
+        else atomicMax(out + i, x);
+      }
+    }
+  }
+}
+
 __host__ __forceinline__ float ord2f_host(unsigned u) {
   unsigned v = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
   float f;

@@ -1147,18 +1147,9 @@ __global__ void k_cell_bounds(const double* __restrict__ cell_enu, int begin, in
   const bool valid = k < count;
   const float x = valid ? (float)cell_enu[3LL * (begin + k)] : 0.f;
   const float y = valid ? (float)cell_enu[3LL * (begin + k) + 1] : 0.f;
-  unsigned mnx = valid ? f2ord(x) : 0xFFFFFFFFu, mny = valid ? f2ord(y) : 0xFFFFFFFFu;
-  unsigned mxx = valid ? f2ord(x) : 0u, mxy = valid ? f2ord(y) : 0u;
-  mnx = __reduce_min_sync(0xffffffffu, mnx);
-  mny = __reduce_min_sync(0xffffffffu, mny);
-  mxx = __reduce_max_sync(0xffffffffu, mxx);
-  mxy = __reduce_max_sync(0xffffffffu, mxy);
-  if ((threadIdx.x & 31) == 0) {
-    atomicMin(&bounds[0], mnx);
-    atomicMin(&bounds[1], mny);
-    atomicMax(&bounds[2], mxx);
-    atomicMax(&bounds[3], mxy);
-  }
+  unsigned b[4] = {valid ? f2ord(x) : 0xFFFFFFFFu, valid ? f2ord(y) : 0xFFFFFFFFu,
+                   valid ? f2ord(x) : 0u, valid ? f2ord(y) : 0u};
+  block_bounds_atomic<2, 2>(b, bounds);
 }
 
 __device__ __forceinline__ uint32_t spread16(uint32_t x) {
