@@ -54,8 +54,16 @@ __global__ void k_mesh_emit(const double* __restrict__ clon, const double* __res
                             double* __restrict__ add_lat, double* __restrict__ add_h) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
-  double ang[6];
-  int cell[6];
+  // Order of the cells around the vertex by the reference's FP64 angle
+  // atan2(dlon, dlat) in [0, 2 pi), stable (sort_index, cpp:137-146). The
+  // order is taken from FP32 angles of the same differences (within 2e-6 rad
+  // of the FP64 angle: argument rounding, atan2f, the 2 pi wrap) when every
+  // gap between sorted angles, and to the wrap at 0 / 2 pi, exceeds
+  // kAngleGap; then it is the FP64 order, with no ties. Otherwise (near-collinear
+  // cells, or a cell due north) the FP64 angles are computed and sorted.
+  constexpr float kAngleGap = 1e-5f;
+  float ang[6];
+  int cell[6], slot_cell[6];
   int n = 0;
   double hsum = 0.0;
   const double lon_v = vlon[v], lat_v = vlat[v];
@@ -63,18 +71,19 @@ __global__ void k_mesh_emit(const double* __restrict__ clon, const double* __res
   for (int j = 0; j < 6; j++) {
     int c = cov[(long long)nv * j + v];
     if (c != -2 && c >= 0 && c < ncell) {
-      double a = atan2(clon[c] - lon_v, clat[c] - lat_v);
-      if (a < 0.0) a += 2.0 * kPi;
+      float a = atan2f((float)(clon[c] - lon_v), (float)(clat[c] - lat_v));
+      if (a < 0.f) a += 2.f * (float)kPi;
       ang[n] = a;
       cell[n] = c;
+      slot_cell[n] = c;
       n++;
       hsum += hsurf[c];
     }
   }
   // Stable insertion sort of (angle, cell) pairs by angle.
   for (int k = 1; k < n; k++) {
-    double a = ang[k];
-    int c = cell[k];
+    const float a = ang[k];
+    const int c = cell[k];
     int m = k - 1;
     while (m >= 0 && a < ang[m]) {
       ang[m + 1] = ang[m];
@@ -83,6 +92,30 @@ __global__ void k_mesh_emit(const double* __restrict__ clon, const double* __res
     }
     ang[m + 1] = a;
     cell[m + 1] = c;
+  }
+  bool clear = n == 0 || (ang[0] > kAngleGap && ang[n - 1] < 2.f * (float)kPi - kAngleGap);
+  for (int k = 1; k < n; k++) clear = clear && ang[k] - ang[k - 1] > kAngleGap;
+  if (!clear) {
+    double a64[6];
+    for (int k = 0; k < n; k++) {
+      const int c = slot_cell[k];
+      double a = atan2(clon[c] - lon_v, clat[c] - lat_v);
+      if (a < 0.0) a += 2.0 * kPi;
+      a64[k] = a;
+      cell[k] = c;
+    }
+    for (int k = 1; k < n; k++) {
+      const double a = a64[k];
+      const int c = cell[k];
+      int m = k - 1;
+      while (m >= 0 && a < a64[m]) {
+        a64[m + 1] = a64[m];
+        cell[m + 1] = cell[m];
+        m--;
+      }
+      a64[m + 1] = a;
+      cell[m + 1] = c;
+    }
   }
   const unsigned long long off = offsets[v];
   long long t = (long long)(off & 0xFFFFFFFFull);
@@ -128,8 +161,11 @@ __global__ void k_mesh_ecef(const double* __restrict__ clon, const double* __res
     } else {
       lon = add_lon[i - ncell]; lat = add_lat[i - ncell]; h = add_h[i - ncell];
     }
-    const double sin_lon = sin(lon), cos_lon = cos(lon);
-    const double sin_lat = sin(lat), cos_lat = cos(lat);
+    // sincos: one argument reduction for both; the same bits as sin and cos
+    // (compared on 2e8 arguments over [-pi, pi] on sm_103a).
+    double sin_lon, cos_lon, sin_lat, cos_lat;
+    sincos(lon, &sin_lon, &cos_lon);
+    sincos(lat, &sin_lat, &cos_lat);
     x = (kEarthRadius + h) * cos_lat * cos_lon;
     y = (kEarthRadius + h) * cos_lat * sin_lon;
     z = (kEarthRadius + h) * sin_lat;
