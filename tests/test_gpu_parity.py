@@ -58,6 +58,31 @@ def test_gpu_mesh_matches_reference_mesh(name):
 
 
 @pytest.mark.parametrize("grid_type", [0, 1])
+def test_gpu_mesh_order_near_ties(small_domain, grid_type):
+    """The mesh kernel orders the cells around a vertex by FP32 angles and
+    falls back to FP64 angles near ties: cells due north or south of a
+    vertex (angle 0 / pi, at the wrap), cells on one line through the vertex
+    (equal angles, stable order) and cells 1e-12 rad off that line give the
+    oracle's triangles."""
+    d = small_domain
+    clon, clat = d.clon.copy(), d.clat.copy()
+    cov = d.cells_of_vertex
+    full = np.where((cov >= 0).all(0))[0]
+    rng = np.random.default_rng(5)
+    picks = rng.choice(full, 30, replace=False)
+    for v in picks[:10]:
+        clon[cov[0, v]] = d.vlon[v]
+    for k, v in enumerate(picks[10:]):
+        c1, c2 = cov[1, v], cov[3, v]
+        clon[c2] = d.vlon[v] + 0.5 * (clon[c1] - d.vlon[v]) + (1e-12 if k % 2 else 0.0)
+        clat[c2] = d.vlat[v] + 0.5 * (clat[c1] - d.vlat[v])
+    inputs = (clon, clat, d.hsurf, d.vlon, d.vlat, cov)
+    enu, vot = mesh_enu32(*inputs, grid_type)
+    _, _, vot_o = oracle.mesh_enu(*inputs, grid_type)
+    np.testing.assert_array_equal(vot, vot_o)
+
+
+@pytest.mark.parametrize("grid_type", [0, 1])
 def test_gpu_enu32_matches_oracle(small_domain, grid_type):
     enu, vot = mesh_enu32(*small_domain.inputs(), grid_type)
     e64, e32, vot_o = oracle.mesh_enu(*small_domain.inputs(), grid_type)
