@@ -255,10 +255,11 @@ struct Capture {
     capturing = e == cudaSuccess;
     return e;
   }
-  // A timing event: recorded as a node of the graph while capturing.
+  // A timing event: recorded as a node of the graph while capturing, else on
+  // the caller's stream, which then carries the work.
   cudaError_t record(cudaEvent_t ev) {
     return capturing ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal)
-                     : cudaEventRecord(ev, s);
+                     : cudaEventRecord(ev, launch);
   }
   // Ends the capture, updates the cached executable graph in place (or
   // instantiates it when the shape changed) and launches it.

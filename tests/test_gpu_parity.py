@@ -351,6 +351,25 @@ def test_gpu_graph_replay_matches_direct_launch(small_domain):
         np.testing.assert_array_equal(sa, sb)
 
 
+def test_gpu_phase_times_without_graph():
+    """Phase times of calls launched without the graph (direct launch, the
+    learned start) bracket their work like those of captured calls: the
+    events are recorded on the stream that carries the work."""
+    torch = pytest.importorskip("torch")
+    from horayzon_extpar_gb300 import horizon_svf_comp_device, learned
+    d = synthetic.make_config("c3", seed=0, box_km=120.0)
+    t = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in d.inputs()]
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    for _ in range(2):
+        _, _, cap = horizon_svf_comp_device(*t, *args)
+        _, _, direct = horizon_svf_comp_device(*t, *args, direct_launch=True)
+        _, _, lrn = horizon_svf_comp_device(*t, *args, mlp_params=learned.init_params(0))
+    assert cap["ms_trace"] > 2.0
+    for st in (direct, lrn):
+        assert 0.7 * cap["ms_trace"] < st["ms_trace"] < 3.0 * cap["ms_trace"]
+        assert 0.5 * cap["ms_bvh"] < st["ms_bvh"] < 3.0 * cap["ms_bvh"]
+
+
 @pytest.mark.parametrize("value", ["ncell", -1, -3])
 def test_gpu_bad_indices_raise_reference_error(small_domain, value):
     """With every other argument valid, the index check of cells_of_vertex
