@@ -30,6 +30,9 @@ def assert_parity(h, s, h_ref, s_ref, min_exact=0.999):
     same = d <= EXACT_DEG
     np.testing.assert_array_equal(h[same], h_ref[same])
     assert np.abs(s - s_ref).max() <= SVF_TOL
+    # Cells whose horizons all agree have the same SVF to rounding.
+    cells = same.all(axis=0)
+    np.testing.assert_allclose(s[cells], s_ref[cells], rtol=0, atol=1e-12)
 
 
 @pytest.fixture(scope="module", autouse=True)
