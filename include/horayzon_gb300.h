@@ -107,10 +107,12 @@ typedef struct hz_stats {
     int64_t tri_tests;       /* with count_work: ray/triangle tests */
     int32_t n_tri;           /* triangles in the mesh (cpp:314-315) */
     int32_t n_mesh_vert;     /* mesh vertices: cells + appended ICON vertices */
+    /* Phase times: CUDA events on the stream that carries the work (nodes
+     * of the call's graph, or the caller's stream when launched directly). */
     double ms_h2d;           /* host->device copies (host entry points) */
     double ms_mesh;          /* mesh assembly + geodetic frames */
     double ms_bvh;           /* LBVH build */
-    double ms_trace;         /* horizon search + SVF */
+    double ms_trace;         /* learned start if any, frames, search, outputs */
     double ms_d2h;           /* device->host copies (host entry points) */
     double ms_total;         /* whole call, wall clock */
     int64_t kernel_launches; /* CUDA kernels this call launched */
