@@ -438,38 +438,6 @@ int validate(int num_cell, int num_vertex, int num_hori, int grid_type, double d
   return HZ_OK;
 }
 
-// mo_lradtopo_horayzon.cpp:624-644 on the host, from the device sum of the
-// cells' ECEF coordinates.
-Frame make_frame(double xo, double yo, double zo) {
-  const double R = kEarthRadius;
-  Frame f;
-  double radius = sqrt(xo * xo + yo * yo + zo * zo);
-  double lon_o = atan2(yo, xo);
-  double lat_o = asin(zo / radius);
-  f.sin_lon = sin(lon_o);
-  f.cos_lon = cos(lon_o);
-  f.sin_lat = sin(lat_o);
-  f.cos_lat = cos(lat_o);
-  f.xe = R * cos(lat_o) * cos(lon_o);
-  f.ye = R * cos(lat_o) * sin(lon_o);
-  f.ze = R * sin(lat_o);
-  f.cyx = (-f.sin_lat) * f.cos_lon;
-  f.cyy = f.sin_lat * f.sin_lon;
-  f.czx = f.cos_lat * f.cos_lon;
-  f.czy = f.cos_lat * f.sin_lon;
-  auto enu = [&](double x, double y, double z) {
-    double dx = x - f.xe, dy = y - f.ye, dz = z - f.ze;
-    double3 r;
-    r.x = (-f.sin_lon) * dx + f.cos_lon * dy;
-    r.y = f.cyx * dx - f.cyy * dy + f.cos_lat * dz;
-    r.z = f.czx * dx + f.czy * dy + f.sin_lat * dz;
-    return r;
-  };
-  f.centre = enu(0.0, 0.0, 0.0);
-  f.pole = enu(0.0, 0.0, R);
-  return f;
-}
-
 __global__ void k_stamp(unsigned long long* t) {
   unsigned long long now;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
@@ -579,7 +547,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   HZ_CUDA(cudaStreamSynchronize(s));
   std::vector<Frame> frames(n);
   for (int d = 0; d < n; d++) {
-    frames[d] = make_frame(sums[3 * d], sums[3 * d + 1], sums[3 * d + 2]);
+    frames[d] = enu_frame_from_sum(sums[3 * d], sums[3 * d + 1], sums[3 * d + 2]);
     const double* so = sums + 3 * d;
     const double radius = sqrt(so[0] * so[0] + so[1] * so[1] + so[2] * so[2]);
     out->origin_lat[d] = rad2deg(asin(so[2] / radius));
@@ -1118,6 +1086,7 @@ const char* hz_last_error(void) { return g_last_error.c_str(); }
 int hz_version(void) { return HZ_VERSION; }
 
 int hz_release_workspace(int device) {
+  static_forget_device(device);
   std::lock_guard<std::mutex> lock(g_engines_mu);
   for (int d = 0; d < 128; d++) {
     if ((device < 0 || d == device) && g_engines[d]) {

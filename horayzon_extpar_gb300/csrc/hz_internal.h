@@ -49,6 +49,9 @@ cudaError_t mesh_ecef(const double* clon, const double* clat, const double* hsur
                       const double* add_lon, const double* add_lat, const double* add_h,
                       int ncell, int nadd, double* ecef, double* block_sums,
                       double* d_origin_sum, cudaStream_t s);
+// cpp:624-644: the domain's ENU frame from the sum of the cells' ECEF
+// coordinates (host, glibc; the one definition every entry point uses).
+Frame enu_frame_from_sum(double xo, double yo, double zo);
 // cpp:178-201: FP32 ENU of every mesh vertex, FP64 ENU of every cell.
 // vert_lo (optional, 3 per mesh vertex): FP64 value minus its FP32 rounding.
 cudaError_t mesh_enu(const double* ecef, int nmv, int ncell, const Frame& f,
@@ -190,6 +193,11 @@ struct TraceKnobs {
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
                        int* work, unsigned long long* counters, int* err, const TraceKnobs& k,
                        bool count_work, bool precise, cudaStream_t s);
+
+// ---- hz_static.cu -----------------------------------------------------------
+// Forgets the cached device address of the no-allocation entry point's
+// static array on `device` (-1: all devices).
+void static_forget_device(int device);
 
 // ---- hz_hostcopy.cu ---------------------------------------------------------
 // Copies between device memory and caller host buffers: page-locked buffers

@@ -288,6 +288,40 @@ cudaError_t mesh_ecef(const double* clon, const double* clat, const double* hsur
   return cudaGetLastError();
 }
 
+// mo_lradtopo_horayzon.cpp:624-644 on the host (glibc), from the device sum
+// of the cells' ECEF coordinates: origin direction, its lon / lat, the
+// rotation terms and the Earth centre and North Pole in ENU. Every entry
+// point builds its frame here, so the FP64 frame is the same bits for all.
+Frame enu_frame_from_sum(double xo, double yo, double zo) {
+  const double R = kEarthRadius;
+  Frame f;
+  const double radius = sqrt(xo * xo + yo * yo + zo * zo);
+  const double lon_o = atan2(yo, xo);
+  const double lat_o = asin(zo / radius);
+  f.sin_lon = sin(lon_o);
+  f.cos_lon = cos(lon_o);
+  f.sin_lat = sin(lat_o);
+  f.cos_lat = cos(lat_o);
+  f.xe = R * cos(lat_o) * cos(lon_o);
+  f.ye = R * cos(lat_o) * sin(lon_o);
+  f.ze = R * sin(lat_o);
+  f.cyx = (-f.sin_lat) * f.cos_lon;
+  f.cyy = f.sin_lat * f.sin_lon;
+  f.czx = f.cos_lat * f.cos_lon;
+  f.czy = f.cos_lat * f.sin_lon;
+  auto enu = [&](double x, double y, double z) {
+    const double dx = x - f.xe, dy = y - f.ye, dz = z - f.ze;
+    double3 r;
+    r.x = (-f.sin_lon) * dx + f.cos_lon * dy;
+    r.y = f.cyx * dx - f.cyy * dy + f.cos_lat * dz;
+    r.z = f.czx * dx + f.czy * dy + f.sin_lat * dz;
+    return r;
+  };
+  f.centre = enu(0.0, 0.0, 0.0);
+  f.pole = enu(0.0, 0.0, R);
+  return f;
+}
+
 cudaError_t mesh_enu(const double* ecef, int nmv, int ncell, const Frame& f, float* vert32,
                      double* cell_enu, float* vert_lo, cudaStream_t s) {
   if (nmv <= 0) return cudaSuccess;

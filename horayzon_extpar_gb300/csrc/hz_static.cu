@@ -13,13 +13,16 @@
 //
 // Host code cannot use the array's name as a device address (it names a
 // host-side shadow), so on the first call on each device, with that device
-// current, cudaGetSymbolAddress resolves the device address; that first call
-// should come before any stream capture. All calls share the array, so GPU
-// work of two calls must never overlap: the entry point holds a process-wide
-// lock and waits for its stream before returning. Values left from the
-// previous call are never read: every counter and flag that must start at
-// zero is cleared on the stream at the start of the call. Failures are
-// reported through hz_last_error() like the other entry points.
+// current, cudaGetSymbolAddress resolves the device address and the address
+// is kept; hz_release_workspace(device) forgets it (call it after a
+// cudaDeviceReset). The function itself cannot run inside a stream capture:
+// it reads results back to the host and waits for its stream mid-call. All
+// calls share the array, so GPU work of two calls must never overlap: the
+// entry point holds a process-wide lock and, on every return after its first
+// queued operation (success or failure), waits for its stream. Values left
+// from the previous call are never read: every counter and flag that must
+// start at zero is cleared on the stream at the start of the call. Failures
+// are reported through hz_last_error() like the other entry points.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -133,41 +136,19 @@ StaticBuffers lay_out(Layout& L, long long ncell, long long nvert, long long max
   return b;
 }
 
-// ENU frame from the summed cell ECEF coordinates (mo_lradtopo_horayzon.cpp:
-// 624-644), with the same expressions as the other entry points.
-Frame frame_from_sum(double xo, double yo, double zo) {
-  const double R = kEarthRadius;
-  Frame f;
-  const double radius = sqrt(xo * xo + yo * yo + zo * zo);
-  const double lon_o = atan2(yo, xo);
-  const double lat_o = asin(zo / radius);
-  f.sin_lon = sin(lon_o);
-  f.cos_lon = cos(lon_o);
-  f.sin_lat = sin(lat_o);
-  f.cos_lat = cos(lat_o);
-  f.xe = R * cos(lat_o) * cos(lon_o);
-  f.ye = R * cos(lat_o) * sin(lon_o);
-  f.ze = R * sin(lat_o);
-  f.cyx = (-f.sin_lat) * f.cos_lon;
-  f.cyy = f.sin_lat * f.sin_lon;
-  f.czx = f.cos_lat * f.cos_lon;
-  f.czy = f.cos_lat * f.sin_lon;
-  auto enu = [&](double x, double y, double z) {
-    const double dx = x - f.xe, dy = y - f.ye, dz = z - f.ze;
-    double3 r;
-    r.x = (-f.sin_lon) * dx + f.cos_lon * dy;
-    r.y = f.cyx * dx - f.cyy * dy + f.cos_lat * dz;
-    r.z = f.czx * dx + f.czy * dy + f.sin_lat * dz;
-    return r;
-  };
-  f.centre = enu(0.0, 0.0, 0.0);
-  f.pole = enu(0.0, 0.0, R);
-  return f;
-}
-
 inline double deg2rad_s(double a) { return ((a / 180.0) * kPi); }
 
 }  // namespace
+
+// Forgets the cached device address of the array on `device` (-1: all): a
+// device reset reloads the module and may place the array elsewhere, so the
+// next call resolves the address again.
+void static_forget_device(int device) {
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  for (int d = 0; d < 128; d++)
+    if (device < 0 || d == device) g_static_addr[d] = nullptr;
+}
+
 }  // namespace hz
 
 using namespace hz;
@@ -201,7 +182,8 @@ extern "C" int hz_horizon_svf_device_static(
     char buf[320];
     snprintf(buf, sizeof(buf),
              "domain needs %zu bytes of scratch, above the fixed %zu-byte static array "
-             "(about 90,000 cells); use hz_horizon_svf_device",
+             "(about 90,000 cells with grid_type 1, 120,000 with grid_type 0, at one "
+             "vertex per two cells); use hz_horizon_svf_device",
              dry.off, kStaticScratchBytes);
     set_last_error(buf);
     return HZ_ERR_VALUE;
@@ -220,6 +202,13 @@ extern "C" int hz_horizon_svf_device_static(
   cudaStream_t s = (cudaStream_t)stream;
   Layout lay{(char*)g_static_addr[dev]};
   const StaticBuffers b = lay_out(lay, num_cell, num_vertex, max_tri, num_azimuths);
+  // From the first queued operation on, every return waits for the stream
+  // (still under the lock), so that no work of a failed call can overlap the
+  // next call's use of the array.
+  struct DrainOnReturn {
+    cudaStream_t s;
+    ~DrainOnReturn() { (void)cudaStreamSynchronize(s); }
+  } drain{s};
 
   // Cleared every call: the array keeps the previous call's contents.
   HZ_STATIC_CUDA(cudaMemsetAsync(b.err, 0, 4 * sizeof(int), s), "clearing error word");
@@ -256,7 +245,7 @@ extern "C" int hz_horizon_svf_device_static(
   HZ_STATIC_CUDA(cudaMemcpyAsync(sum, b.origin_sum, sizeof(sum), cudaMemcpyDeviceToHost, s),
                  "reading the ECEF sum");
   HZ_STATIC_CUDA(cudaStreamSynchronize(s), "ECEF");
-  const Frame fr = frame_from_sum(sum[0], sum[1], sum[2]);
+  const Frame fr = enu_frame_from_sum(sum[0], sum[1], sum[2]);
   HZ_STATIC_CUDA(mesh_enu(b.ecef, nmv, num_cell, fr, b.vert32, b.cell_enu, nullptr, s), "ENU");
 
   // BVH and search (cpp:395-432, 651-761).

@@ -279,14 +279,20 @@ int hz_mesh_enu32(const double* clon, const double* clat, const double* hsurf,
  * on a shared GPU that cannot afford the device-wide synchronisation of
  * cudaMalloc/cudaFree. It allocates nothing: all intermediate data lives in
  * one fixed 64 MiB __device__ array inside the library (held by every GPU
- * that loads it until the process exits), which limits a domain to about
- * 90,000 cells; larger domains are rejected with HZ_ERR_VALUE and a message
- * naming the limit. The first call on a device resolves the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture. All calls share the array: calls whose GPU
- * work overlapped would race on it, so the function serialises its callers
- * and returns after its work on `stream` has finished. The down-walk bound is
- * the reference's -85 deg; errors are reported through hz_last_error().
+ * that loads it until the process exits). That limits a domain to about
+ * 90,000 cells with grid_type 1 and 120,000 with grid_type 0, at ICON's ratio
+ * of one vertex per two cells (the scratch is about 700 bytes per cell, or
+ * 540 with grid_type 0); larger domains are rejected with HZ_ERR_VALUE and a
+ * message naming the limit. The first call on a device resolves the array's
+ * device address (cudaGetSymbolAddress) with that device current and keeps
+ * it; after a cudaDeviceReset call hz_release_workspace(device), which
+ * forgets it. The function cannot be called while `stream` is being
+ * captured: it reads results back to the host and waits for the stream
+ * mid-call. All calls share the array: calls whose GPU work overlapped would
+ * race on it, so the function serialises its callers, and every return after
+ * its first queued operation (success or error) waits for the work on
+ * `stream` to finish. The down-walk bound is the reference's -85 deg; errors
+ * are reported through hz_last_error().
  */
 int hz_horizon_svf_device_static(const double* clon, const double* clat,
                                  const double* hsurf, const double* vlon,
@@ -321,7 +327,8 @@ const char* hz_last_error(void);
 /* HZ_VERSION of the loaded library. */
 int hz_version(void);
 
-/* Frees the cached device workspace of `device` (-1 = all devices). */
+/* Frees the cached device workspace of `device` (-1 = all devices) and
+ * forgets the cached address of hz_horizon_svf_device_static's array there. */
 int hz_release_workspace(int device);
 
 #ifdef __cplusplus

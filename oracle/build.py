@@ -6,9 +6,10 @@ TEST INFRASTRUCTURE (see ``oracle/__init__.py``).
   ``oracle/_build/libhz_oracle.so`` with ``-ffp-contract=off`` so that no
   multiply-add is fused (the CUDA path rounds every operation the same way).
 * ``build_reference(src)`` compiles the reference's own
-  ``mo_lradtopo_horayzon.cpp`` where it lies (``src``), unmodified, against
+  ``mo_lradtopo_horayzon.cpp`` where it lies (``src``, or the folder named
+  by the environment variable ``HZ_REFERENCE_SRC``), unmodified, against
   ``shim/`` plus ``ref_entry.cpp`` into ``oracle/_ref/libhorayzon_ref.so``.
-  It is skipped when the reference tree is absent.
+  It is skipped when no reference tree is given or found there.
 """
 import os
 import subprocess
@@ -19,7 +20,6 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "libhz_oracle.so")
 REF_SO = os.path.join(REF_DIR, "libhorayzon_ref.so")
-DEFAULT_REFERENCE_SRC = "/root/reference"
 
 _CFLAGS = ["-O3", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
            "-fno-fast-math"]
@@ -52,7 +52,11 @@ def build_oracle(force=False):
 
 
 def reference_source(src=None):
-    src = src or os.environ.get("HZ_REFERENCE_SRC", DEFAULT_REFERENCE_SRC)
+    """The reference tree: ``src``, else $HZ_REFERENCE_SRC; None when neither
+    holds mo_lradtopo_horayzon.cpp."""
+    src = src or os.environ.get("HZ_REFERENCE_SRC")
+    if not src:
+        return None
     cpp = os.path.join(src, "mo_lradtopo_horayzon.cpp")
     return src if os.path.exists(cpp) else None
 
@@ -82,5 +86,7 @@ def build_reference(src=None, force=False):
 
 
 if __name__ == "__main__":
+    # python oracle/build.py [--force] [REFERENCE_TREE]
+    tree = [a for a in sys.argv[1:] if not a.startswith("--")]
     print(build_oracle(force="--force" in sys.argv))
-    print(build_reference(force="--force" in sys.argv))
+    print(build_reference(tree[0] if tree else None, force="--force" in sys.argv))

@@ -1,13 +1,13 @@
 """Generate the border-distance fixture from the reference's own function.
 
 Runs functions.distance_to_border (functions.py:58-97) of the reference tree
-(default /root/reference, or HZ_REFERENCE_SRC) on seeded synthetic domains and
+(the first argument, or HZ_REFERENCE_SRC) on seeded synthetic domains and
 stores inputs and outputs in border_golden.npz. functions.py imports pyproj at
 module level for an unrelated function (observer_perspective); pyproj is not
 installed here, so an empty stand-in module is registered under that name
 before the import (distance_to_border itself uses only numpy and scipy).
 
-    python tests/golden/make_border_golden.py
+    python tests/golden/make_border_golden.py REFERENCE_TREE
 """
 import importlib.util
 import os
@@ -28,7 +28,10 @@ CASES = {"a": dict(edge_km=2.5, box_km=80.0, seed=21),
 
 
 def load_reference_functions():
-    src = os.environ.get("HZ_REFERENCE_SRC", "/root/reference")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HZ_REFERENCE_SRC")
+    if not src:
+        raise SystemExit("pass the reference tree as the first argument or set "
+                         "HZ_REFERENCE_SRC")
     if "pyproj" not in sys.modules:
         stub = types.ModuleType("pyproj")
         stub.Transformer = None

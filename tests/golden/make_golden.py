@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
-Run in a container that has the reference tree (default /root/reference, or
-HZ_REFERENCE_SRC). For every case it builds a seeded synthetic domain and
+Run where the reference tree is, naming it with HZ_REFERENCE_SRC or as the
+first argument. For every case it builds a seeded synthetic domain and
 records the inputs, the outputs of the unmodified reference
 (mo_lradtopo_horayzon.cpp compiled against the project's Embree/TBB
 stand-ins, oracle/_ref) and the reference's triangle mesh
@@ -9,7 +9,7 @@ stand-ins, oracle/_ref) and the reference's triangle mesh
 pure-Python builders (development.py:27-179), loaded function by function
 because that module imports xarray at the top.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py REFERENCE_TREE
 """
 import ast
 import os
@@ -59,10 +59,11 @@ def load_development_builders(src):
 
 
 def main():
-    src = build.reference_source()
+    src = build.reference_source(sys.argv[1] if len(sys.argv) > 1 else None)
     if src is None:
-        raise SystemExit("reference sources not found")
-    build.build_reference()
+        raise SystemExit("reference sources not found: pass the reference tree as the "
+                         "first argument or set HZ_REFERENCE_SRC")
+    build.build_reference(src)
     tm_circ, tm_circ_vert = load_development_builders(src)
     for name, (dkw, args) in CASES.items():
         dom = synthetic.make_domain(**dkw)

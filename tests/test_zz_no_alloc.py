@@ -53,6 +53,55 @@ def test_static_entry_matches_device_entry_two_calls():
         assert np.abs(sn - s_ref.cpu().numpy()).max() <= SVF_TOL
 
 
+def test_static_entry_after_a_failed_call():
+    """A call that fails part way (a cells_of_vertex index out of range,
+    found by the mesh stage on the GPU) returns HZ_ERR_INDEX; the next valid
+    call, which starts from what the failed call left in the array, matches
+    hz_horizon_svf_device."""
+    torch = pytest.importorskip("torch")
+    L = _lib.load()
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream(dev)
+    dom = synthetic.make_domain(edge_km=1.5, box_km=60.0, seed=33)
+    args = (24, 1, 30000.0, 0.2, 1, 2)
+    t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in dom.inputs()]
+    bad = t[5].clone()
+    bad[2, dom.nvertex // 2] = dom.ncell + 7
+    h = torch.full((args[0], dom.ncell), float("nan"), dtype=torch.float64, device=dev)
+    s = torch.full((dom.ncell,), float("nan"), dtype=torch.float64, device=dev)
+    rc = _static_call(L, t[:5] + [bad], h, s, dom.ncell, dom.nvertex, args, stream)
+    assert rc == _lib.HZ_ERR_INDEX
+    assert "out of range" in _lib.last_error()
+    h_ref, s_ref, _ = horizon_svf_comp_device(*t, *args)
+    rc = _static_call(L, t, h, s, dom.ncell, dom.nvertex, args, stream)
+    assert rc == _lib.HZ_OK, _lib.last_error()
+    torch.cuda.synchronize()
+    assert np.abs(h.cpu().numpy() - h_ref.cpu().numpy()).max() <= EXACT_DEG
+    assert np.abs(s.cpu().numpy() - s_ref.cpu().numpy()).max() <= SVF_TOL
+
+
+def test_static_entry_accepts_the_documented_domain_size():
+    """A domain of about 90,000 cells (grid_type 1, one vertex per two
+    cells) fits the array, and its results match hz_horizon_svf_device."""
+    torch = pytest.importorskip("torch")
+    L = _lib.load()
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream(dev)
+    dom = synthetic.make_domain(edge_km=1.0, box_km=200.0, seed=34)
+    assert 85_000 <= dom.ncell <= 100_000, dom.ncell
+    assert dom.nvertex <= dom.ncell // 2 + dom.ncell // 50
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in dom.inputs()]
+    h = torch.empty((args[0], dom.ncell), dtype=torch.float64, device=dev)
+    s = torch.empty(dom.ncell, dtype=torch.float64, device=dev)
+    rc = _static_call(L, t, h, s, dom.ncell, dom.nvertex, args, stream)
+    assert rc == _lib.HZ_OK, _lib.last_error()
+    h_ref, s_ref, _ = horizon_svf_comp_device(*t, *args)
+    torch.cuda.synchronize()
+    assert np.abs(h.cpu().numpy() - h_ref.cpu().numpy()).max() <= EXACT_DEG
+    assert np.abs(s.cpu().numpy() - s_ref.cpu().numpy()).max() <= SVF_TOL
+
+
 def test_static_entry_refuses_domains_above_its_limit():
     torch = pytest.importorskip("torch")
     L = _lib.load()
