@@ -254,42 +254,70 @@ def precision_report(d_in, h_ref, stream):
             "local_frame_trace_ms": st["ms_trace"]}
 
 
-def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args, sample=None):
-    """Learned warm start vs the plain chained search on the same workload.
-
-    The MLP is trained first (untimed) on the plain method's horizons of 8
-    other terrain seeds of the same recipe (120 x 120 km boxes), on the GPU with
-    the library's own kernels."""
+def train_mlp(make_dom, args=ARGS, n_seeds=8, samples_per_seed=1_000_000, steps=3000,
+              batch=32768):
+    """Trains the warm-start MLP (untimed) on the plain method's horizons of
+    n_seeds other terrain seeds, on the GPU with the library's own kernels.
+    make_dom(i) builds the i-th training domain."""
     import torch
 
-    from horayzon_extpar_gb300 import horizon_svf_comp_device, learned, synthetic
+    from horayzon_extpar_gb300 import learned
     t0 = time.perf_counter()
     Xs, Ts = [], []
-    for seed in range(1, 9):
-        d = synthetic.make_config("c3", seed=1000 + seed, box_km=min(120.0, args.box_km))
-        X, T = learned.training_samples(d, ARGS, max_samples=1_000_000, seed=seed)
+    for i in range(n_seeds):
+        X, T = learned.training_samples(make_dom(i), args, max_samples=samples_per_seed,
+                                        seed=i + 1)
         Xs.append(X)
         Ts.append(T)
     X, T = torch.cat(Xs), torch.cat(Ts)
-    params, hist = learned.train(X, T, steps=3000, batch=32768, lr=2e-3, seed=0,
-                                 log_every=1000)
+    n = int(X.shape[0])
+    params, hist = learned.train(X, T, steps=steps, batch=batch, lr=2e-3, seed=0,
+                                 log_every=max(1, steps // 3))
     del X, T, Xs, Ts
-    train_s = time.perf_counter() - t0
-    out = {"training": {"seeds": "8 other seeds, 120 x 120 km boxes of the same recipe",
-                        "samples": 8_000_000, "steps": 3000, "batch": 32768,
-                        "seconds": train_s, "loss_history": hist}}
+    return params, {"samples": n, "steps": steps, "batch": batch,
+                    "seconds": time.perf_counter() - t0, "loss_history": hist}
+
+
+def auto_groups(ncell: int, nhori: int) -> int:
+    """The library's choice for mlp_azimuth_groups = -1 (hz_options): the
+    smallest divisor G of nhori with ncell x G >= 4 x the GPU's resident
+    threads (SMs x 1024), else nhori."""
+    import torch
+    target = 4 * torch.cuda.get_device_properties(0).multi_processor_count * 1024
+    for g in range(1, nhori + 1):
+        if nhori % g == 0 and ncell * g >= target:
+            return g
+    return nhori
+
+
+LEARNED_MODES = {"first_azimuth": dict(),
+                 "every_azimuth": dict(mlp_every_azimuth=True),
+                 "azimuth_groups_auto": dict(mlp_azimuth_groups=-1)}
+
+
+def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args, sample=None):
+    """Learned warm start vs the plain chained search on the headline workload
+    (timed like the plain steps: CUDA events around each call). The MLP is
+    trained on 8 other seeds of the same recipe (120 x 120 km boxes).
+    Returns the report and the trained parameters."""
+    import torch
+
+    from horayzon_extpar_gb300 import horizon_svf_comp_device, synthetic
+    params, info = train_mlp(lambda i: synthetic.make_config(
+        "c3", seed=1001 + i, box_km=min(120.0, args.box_km)))
+    info["seeds"] = "8 other seeds, 120 x 120 km boxes of the same recipe"
+    out = {"training": info}
     evals = dom.ncell * ARGS[0]
-    for mode, every in (("first_azimuth", False), ("every_azimuth", True)):
+    for mode, kw in LEARNED_MODES.items():
         for _ in range(max(1, args.warmup)):
-            horizon_svf_comp_device(*d_in, *ARGS, stream=stream, mlp_params=params,
-                                    mlp_every_azimuth=every)
+            horizon_svf_comp_device(*d_in, *ARGS, stream=stream, mlp_params=params, **kw)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(args.steps)]
         rays = 0
         for k in range(args.steps):
             ev[k][0].record(stream)
             h, s, st = horizon_svf_comp_device(*d_in, *ARGS, stream=stream, mlp_params=params,
-                                               mlp_every_azimuth=every)
+                                               **kw)
             ev[k][1].record(stream)
             rays = st["num_rays"]
         torch.cuda.synchronize()
@@ -303,8 +331,62 @@ def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args, sample=None)
                          "frac_identical": float(np.mean(dh <= 1e-9)),
                          "frac_cells_svf_within_1e-3": float(np.mean(ds <= 1e-3)),
                          "max_abs_svf": float(ds.max())}}
+        if mode == "azimuth_groups_auto":
+            out[mode]["groups"] = auto_groups(dom.ncell, ARGS[0])
         if sample is not None:
             out[mode]["parity"] = parity_block(h.cpu().numpy(), s.cpu().numpy(), sample)
+    return out, params
+
+
+def learned_small_report(stream, reps=5, parity_cells=20000):
+    """The learned start where the plain chain under-fills the GPU: the
+    2.5 km / 400 km domain (57k cells; the chain gives one lane per cell and
+    its 24 azimuths run one after another) and the 100 m / 150 km domain of
+    the learned configuration, each with an MLP trained on 8 other seeds of
+    its own recipe. Per mode: best of `reps` calls (search phase, including
+    the learned start's raster, features and MLP, and the whole call on
+    device-resident inputs), rays per evaluation, and parity against the
+    oracle on a cell sample."""
+    import torch
+
+    from horayzon_extpar_gb300 import horizon_svf_comp_device, synthetic
+    cases = [("c1", "2.5 km grid, 400x400 km, nhori 24",
+              lambda i: synthetic.make_config("c1", seed=2001 + i, box_km=200.0)),
+             ("c4", "100 m grid, 150x150 km, nhori 24",
+              lambda i: synthetic.make_config("c4", seed=3001 + i, box_km=25.0))]
+    out = {}
+    for key, desc, make_train in cases:
+        params, info = train_mlp(make_train, samples_per_seed=500_000)
+        d = synthetic.make_config(key, seed=0)
+        t = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in d.inputs()]
+        evals = d.ncell * ARGS[0]
+        res = {"workload": desc, "ncell": d.ncell, "training": info}
+        modes = {"plain": None, "first_azimuth": {}, "azimuth_groups_auto":
+                 {"mlp_azimuth_groups": -1}}
+        sample = oracle_sample(d, ARGS, parity_cells) if parity_cells > 0 else None
+        for mode, kw in modes.items():
+            extra = {} if kw is None else dict(mlp_params=params, **kw)
+            horizon_svf_comp_device(*t, *ARGS, stream=stream, **extra)  # warm-up
+            best = None
+            for _ in range(reps):
+                h, s, st = horizon_svf_comp_device(*t, *ARGS, stream=stream, **extra)
+                if best is None or st["ms_trace"] < best["ms_trace"]:
+                    best = st
+            call_ms = best["ms_mesh"] + best["ms_bvh"] + best["ms_trace"]
+            res[mode] = {"search_ms": best["ms_trace"], "call_ms": call_ms,
+                         "evals_per_s_search": evals / (best["ms_trace"] * 1e-3),
+                         "evals_per_s_call": evals / (call_ms * 1e-3),
+                         "rays_per_eval": best["num_rays"] / evals}
+            if mode == "azimuth_groups_auto":
+                res[mode]["groups"] = auto_groups(d.ncell, ARGS[0])
+            if sample is not None:
+                res[mode]["parity"] = parity_block(h.cpu().numpy(), s.cpu().numpy(), sample)
+        for mode in ("first_azimuth", "azimuth_groups_auto"):
+            res[mode]["speedup_vs_plain_search"] = (res["plain"]["search_ms"] /
+                                                    res[mode]["search_ms"])
+            res[mode]["speedup_vs_plain_call"] = res["plain"]["call_ms"] / res[mode]["call_ms"]
+        out[key] = res
+        del t
     return out
 
 
@@ -326,26 +408,38 @@ def drop_in_report(dom, steps):
                                               "ms_d2h")}}
 
 
-def batch_report(args):
-    """64 uneven independent domains in one call (one persistent search)."""
+def batch_report(args, mlp_params=None):
+    """64 uneven independent domains in one call (one persistent search);
+    with mlp_params also the same batch with the learned start (the
+    library's choice of azimuth groups)."""
     from horayzon_extpar_gb300 import synthetic
     from horayzon_extpar_gb300.horizon_svf import horizon_svf_comp_batch
     batch = synthetic.make_batch(64, seed=0)
     doms = [(d.inputs(), a) for d, a in batch]
     evals = sum(d.ncell * a[0] for d, a in batch)
-    horizon_svf_comp_batch(doms)  # warm-up
-    t0 = time.perf_counter()
-    _, st = horizon_svf_comp_batch(doms, return_stats=True)
-    wall = time.perf_counter() - t0
-    lat = np.array(st["latency_ms"])
-    return {"workload": "64 domains, 10k-500k cells (log-uniform), 0.5-2.5 km, relief "
-                        "1000-4500 m, nhori in {16, 24, 36}",
-            "cells": int(sum(d.ncell for d, _ in batch)), "evals": int(evals),
-            "search_ms": st["ms_trace"], "evals_per_s_search": evals / (st["ms_trace"] * 1e-3),
-            "evals_per_s_e2e_host": evals / wall,
-            "latency_ms_p50": float(np.percentile(lat, 50)),
-            "latency_ms_p99": float(np.percentile(lat, 99)),
-            "kernel_launches": st["kernel_launches"]}
+
+    def run(**kw):
+        horizon_svf_comp_batch(doms, **kw)  # warm-up
+        t0 = time.perf_counter()
+        _, st = horizon_svf_comp_batch(doms, return_stats=True, **kw)
+        wall = time.perf_counter() - t0
+        lat = np.array(st["latency_ms"])
+        return {"search_ms": st["ms_trace"],
+                "evals_per_s_search": evals / (st["ms_trace"] * 1e-3),
+                "evals_per_s_e2e_host": evals / wall,
+                "rays_per_eval": st["num_rays"] / evals,
+                "latency_ms_p50": float(np.percentile(lat, 50)),
+                "latency_ms_p99": float(np.percentile(lat, 99)),
+                "kernel_launches": st["kernel_launches"]}
+
+    out = {"workload": "64 domains, 10k-500k cells (log-uniform), 0.5-2.5 km, relief "
+                       "1000-4500 m, nhori in {16, 24, 36}",
+           "cells": int(sum(d.ncell for d, _ in batch)), "evals": int(evals)}
+    out.update(run())
+    if mlp_params is not None:
+        out["learned"] = run(mlp_params=mlp_params, mlp_azimuth_groups=-1)
+        out["learned"]["mlp"] = "trained on the 500 m recipe (headline workload's MLP)"
+    return out
 
 
 def configs_report(dom, d_in, stream, reps=2, parity_cells=20000):
@@ -552,9 +646,11 @@ def run_gpu(args):
     # configurations, each compared with the oracle on a cell sample.
     extras = {}
     if not args.no_extras and rank == 0:
-        extras["learned"] = learned_report(dom, d_in, hz, sv, stream, ms, args, sample)
+        extras["learned"], mlp = learned_report(dom, d_in, hz, sv, stream, ms, args, sample)
+        extras["learned_small_domains"] = learned_small_report(
+            stream, parity_cells=args.parity_cells)
         extras["precision"] = precision_report(d_in, hz, stream)
-        extras["batched_domains"] = batch_report(args)
+        extras["batched_domains"] = batch_report(args, mlp)
         extras["drop_in_numpy"] = drop_in_report(dom, min(args.steps, 3))
         extras["configs"] = configs_report(dom, d_in, stream,
                                            parity_cells=args.parity_cells)

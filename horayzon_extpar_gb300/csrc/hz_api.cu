@@ -103,6 +103,7 @@ struct Problem {
   double dist_search, ray_org_elev;
   int refine, svf_type;
   int cell_begin, cell_count;  // traced range
+  int groups;                  // search items per traced cell (DomainDesc::groups)
 };
 
 // Device buffers of one domain.
@@ -124,6 +125,7 @@ struct Buffers {
   float* rz;
   long long raster_budget;
   int16_t* start_m;
+  double* svf_part;    // split learned start with refine_factor > 1: [groups][ncell]
   double* cell_enu;
   double* cell_frame;  // [9][ncell] (persistent search)
   float* cell_origin;  // [6][ncell]
@@ -149,7 +151,7 @@ int trace_variant(const hz_options& opt) {
 
 Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhori,
                      int grid_type, bool host_io, bool precise = false, bool learned = false,
-                     long long L = 0, bool wide = false) {
+                     long long L = 0, bool wide = false, long long svf_part_len = 0) {
   Buffers b;
   std::memset(&b, 0, sizeof(b));
   const long long max_tri = (grid_type == 0 ? 4 : 6) * nvert;
@@ -193,6 +195,7 @@ Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhor
     b.rz = c.take<float>(b.raster_budget);
     b.start_m = c.take<int16_t>(L * ncell);
   }
+  if (svf_part_len > 0) b.svf_part = c.take<double>(svf_part_len);
   b.bvh.keys = c.take<uint32_t>(nt);
   b.bvh.vals = c.take<int32_t>(nt);
   b.bvh.keys_alt = c.take<uint32_t>(nt);
@@ -677,7 +680,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
         rdesc[d] = R;
       }
     }
-    long long total = 0;
+    long long total = 0, total_items = 0;
     Fork fk(E, s, learned ? 1 : n);  // the learned start's kernels stay on s
     HZ_CUDA(fk.begin());
     for (int d = 0; d < n; d++) {
@@ -699,9 +702,16 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
         q.cell_count = P.cell_count;
         q.nhori = P.nhori;
         q.L = L;
-        // Predictions feed the first azimuth only unless every azimuth uses
-        // them; features for training cover every azimuth.
-        q.L_pred = (opt.features != nullptr && n == 1) || opt.mlp_every_azimuth ? L : 1;
+        // Predictions feed the first azimuth of each search item (of the
+        // cell's chain, or of each of its azimuth groups) unless every
+        // azimuth uses them; features for training cover every azimuth.
+        if ((opt.features != nullptr && n == 1) || opt.mlp_every_azimuth) {
+          q.n_pred = L;
+          q.a_stride = 1;
+        } else {
+          q.n_pred = P.groups;
+          q.a_stride = L / P.groups;
+        }
         q.dist_search = (float)P.dist_search;
         q.azim_cs = b[d].azim_cs;
         q.raster = rdesc[d];
@@ -731,6 +741,9 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.done = n > 1 ? bb.done + 2 * d : nullptr;
       D.start_m = opt.mlp_params ? b[d].start_m : nullptr;
       D.start_all = opt.mlp_every_azimuth ? 1 : 0;
+      D.groups = P.groups;
+      D.item_begin = total_items;
+      D.svf_part = b[d].svf_part;
       D.raw_j = n == 1 ? opt.raw_index : nullptr;
       D.centre = frames[d].centre;
       D.pole = frames[d].pole;
@@ -750,10 +763,12 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.tfar = (float)P.dist_search;
       desc[d] = D;
       total += P.cell_count;
+      total_items += (long long)P.cell_count * P.groups;
     }
     HZ_CUDA(fk.end());
-    if (total > INT32_MAX - (1ll << 26))
-      return fail(HZ_ERR_VALUE, "more than 2^31 - 2^26 cells in one call");
+    if (total_items > INT32_MAX - (1ll << 26))
+      return fail(HZ_ERR_VALUE, "more than 2^31 - 2^26 search items (cells x azimuth groups) "
+                                "in one call");
     HZ_CUDA(cudaMemcpyAsync(bb.doms, desc, sizeof(DomainDesc) * (size_t)n,
                             cudaMemcpyHostToDevice, s));
     const int adv =
@@ -764,8 +779,9 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     note_launches(1);
     HZ_CUDA(cudaGetLastError());
     const TraceKnobs knobs{adv, leaf, opt.queue_chunk, variant};
-    HZ_CUDA(trace_flat(bb.doms, n, bb.order, (int)total, bb.work, bb.counters, bb.err, knobs,
-                       opt.count_work != 0, b[0].tri_lo != nullptr, s));
+    HZ_CUDA(trace_flat(bb.doms, n, bb.order, (int)total, (int)total_items, bb.work,
+                       bb.counters, bb.err, knobs, opt.count_work != 0,
+                       b[0].tri_lo != nullptr, s));
   }
   HZ_CUDA(cap.record(E.ev[3]));
   phase.next("hz: readback");
@@ -919,6 +935,50 @@ int unstage_outputs(Engine& E, const hz_domain& h, const Buffers& b, int begin, 
   return HZ_OK;
 }
 
+// Search items per traced cell for each domain (DomainDesc::groups) from
+// hz_options.mlp_azimuth_groups: 1 without a learned start or for 0 / 1; an
+// explicit G must divide every domain's num_hori; -1 picks, per domain, the
+// smallest divisor G of num_hori that gives the call at least
+// kItemsPerLane x the GPU's resident lanes of search items (num_hori when
+// none does), so that small domains spread each cell's azimuths over G lanes
+// while domains that fill the GPU keep the reference's chain.
+constexpr int kItemsPerLane = 4;
+
+int azimuth_groups(const hz_domain* doms, int n, const hz_options& opt, int* groups) {
+  for (int d = 0; d < n; d++) groups[d] = 1;
+  const int G = opt.mlp_azimuth_groups;
+  if (opt.mlp_params == nullptr || opt.mlp_every_azimuth || G == 0 || G == 1) return HZ_OK;
+  if (G > 1) {
+    for (int d = 0; d < n; d++) {
+      if (doms[d].num_hori % G != 0)
+        return fail(HZ_ERR_VALUE, "mlp_azimuth_groups %d does not divide num_hori %d", G,
+                    doms[d].num_hori);
+      groups[d] = G;
+    }
+    return HZ_OK;
+  }
+  if (G != -1) return fail(HZ_ERR_VALUE, "mlp_azimuth_groups must be -1, 0 or >= 1");
+  int dev = 0, sms = 0, threads = 0;
+  HZ_CUDA(cudaGetDevice(&dev));
+  HZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  HZ_CUDA(cudaDeviceGetAttribute(&threads, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
+  const long long target = (long long)kItemsPerLane * sms * std::min(threads, 1024);
+  long long cells = 0;
+  for (int d = 0; d < n; d++)
+    cells += opt.cell_count > 0 && n == 1 ? opt.cell_count : doms[d].num_cell;
+  for (int d = 0; d < n; d++) {
+    const int nh = doms[d].num_hori;
+    int pick = nh;
+    for (int g = 1; g <= nh; g++)
+      if (nh % g == 0 && cells * g >= target) {
+        pick = g;
+        break;
+      }
+    groups[d] = pick;
+  }
+  return HZ_OK;
+}
+
 // Shared implementation of the host / device, single / batch entry points.
 int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
               const hz_options& opt, hz_stats* stats) {
@@ -957,11 +1017,18 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
   const bool wide = opt.kernel != HZ_KERNEL_PER_CELL && trace_variant(opt) == kTraceWide;
   if ((opt.raw_index || opt.features) && (n != 1 || !on_device))
     return fail(HZ_ERR_VALUE, "raw_index / features are outputs of the device entry point");
+  std::vector<int> groups(n, 1);
+  rc = azimuth_groups(doms, n, opt, groups.data());
+  if (rc) return rc;
+  auto svf_part_len = [&](int d) {
+    return groups[d] > 1 && doms[d].refine_factor > 1
+               ? (long long)groups[d] * doms[d].num_cell : 0ll;
+  };
   Carver dry(nullptr);
   for (int d = 0; d < n; d++)
     carve_domain(dry, doms[d].num_cell, doms[d].num_vertex, doms[d].num_hori,
                  doms[d].grid_type, !on_device, precise, learned,
-                 (long long)doms[d].num_hori * doms[d].refine_factor, wide);
+                 (long long)doms[d].num_hori * doms[d].refine_factor, wide, svf_part_len(d));
   carve_batch(dry, n, total_cells);
   rc = E->reserve(dry.off, s);
   if (rc) return rc;
@@ -970,7 +1037,8 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
   for (int d = 0; d < n; d++)
     b[d] = carve_domain(c, doms[d].num_cell, doms[d].num_vertex, doms[d].num_hori,
                         doms[d].grid_type, !on_device, precise, learned,
-                        (long long)doms[d].num_hori * doms[d].refine_factor, wide);
+                        (long long)doms[d].num_hori * doms[d].refine_factor, wide,
+                        svf_part_len(d));
   const BatchBuffers bb = carve_batch(c, n, total_cells);
 
   std::vector<Problem> pr(n);
@@ -1002,6 +1070,7 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
     P.svf_type = h.svf_type;
     rc = cell_range(opt, h.num_cell, &P.cell_begin, &P.cell_count);
     if (rc) return rc;
+    P.groups = groups[d];
   }
   double ms_h2d = 0.0;
   if (!on_device) {

@@ -151,9 +151,15 @@ struct DomainDesc {
   const double2* azim_cs;     // lattice tables (trace_tables)
   const double2* elev_cs;
   const double* svf_lattice;
-  unsigned long long* done;   // optional: [0] finished cells, [1] globaltimer at the last
+  unsigned long long* done;   // optional: [0] finished items, [1] globaltimer at the last
   const int16_t* start_m;     // optional learned start lattice index [L][ncell]
-  int start_all;              // 1: learned start at every azimuth; 0: azimuth 0 only
+  int start_all;              // 1: learned start at every azimuth; 0: at each item's first
+  // Search items per traced cell: 1 = the reference's chain over all L
+  // azimuths; G > 1 = G groups of L / G consecutive azimuths (a multiple of
+  // refine), each starting at the learned proposal of its first azimuth.
+  int groups;
+  long long item_begin;       // first search item of this domain (items: groups x cells)
+  double* svf_part;           // groups > 1 and refine > 1: [groups][ncell] SVF sums
   int16_t* raw_j;             // optional output: unclipped horizon j (h = j * 0.25 deg)
   double3 centre, pole;       // Earth centre / North Pole in ENU
   double ray_org_elev, hori_acc, elev_floor;
@@ -190,9 +196,11 @@ struct TraceKnobs {
   int chunk;        // work ids a warp claims per atomic (< 1: kDefaultChunk)
   int variant;      // kTrace*
 };
+// `total` traced cells (frames, epilogue) and `total_items` search items
+// (the sum of groups x traced cells over the domains).
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
-                       int* work, unsigned long long* counters, int* err, const TraceKnobs& k,
-                       bool count_work, bool precise, cudaStream_t s);
+                       int total_items, int* work, unsigned long long* counters, int* err,
+                       const TraceKnobs& k, bool count_work, bool precise, cudaStream_t s);
 
 // ---- hz_static.cu -----------------------------------------------------------
 // Forgets the cached device address of the no-allocation entry point's
@@ -231,7 +239,7 @@ struct LearnParams {
   double3 centre, pole;
   double ray_org_elev;
   int ncell, cell_begin, cell_count, nhori, L;
-  int L_pred;        // azimuths 0 .. L_pred - 1 get features / predictions
+  int n_pred, a_stride;  // azimuths q * a_stride, q < n_pred, get features / predictions
   float dist_search;
   const double2* azim_cs;
   RasterDesc raster;

@@ -273,6 +273,8 @@ extern "C" int hz_horizon_svf_device_static(
   D.two_ha = 2.0 * D.hori_acc;
   D.elev_floor = deg2rad_s(-85.0);
   D.cell_offset = 0;
+  D.groups = 1;
+  D.item_begin = 0;
   D.root = n_tri > 0 ? 0 : kEmptyRef;
   D.n_tri = n_tri;
   D.ncell = num_cell;
@@ -290,8 +292,8 @@ extern "C" int hz_horizon_svf_device_static(
   HZ_STATIC_CUDA(trace_tables(b.azim_cs, b.elev_cs, b.svf_lattice, L, azim_shift, D.hori_acc,
                               D.svf_type, s), "lattice tables");
   const TraceKnobs knobs{kDefaultAdvanceMin, kDefaultLeafMin, kDefaultChunk, kTraceBinary};
-  HZ_STATIC_CUDA(trace_flat(b.dom, 1, b.order, num_cell, b.work, b.counters, b.err, knobs,
-                            false, false, s), "horizon search");
+  HZ_STATIC_CUDA(trace_flat(b.dom, 1, b.order, num_cell, num_cell, b.work, b.counters, b.err,
+                            knobs, false, false, s), "horizon search");
   HZ_STATIC_CUDA(cudaMemcpyAsync(&err, b.err, sizeof(int), cudaMemcpyDeviceToHost, s),
                  "reading error word");
   HZ_STATIC_CUDA(cudaStreamSynchronize(s), "horizon search");

@@ -604,18 +604,35 @@ __device__ __forceinline__ int domain_of(const DomainDesc* __restrict__ doms, in
   return lo;
 }
 
-// One step of a cell's bracketing search (mo_lradtopo_horayzon.cpp:490-555,
-// 694-754) on the state `st` (FP64: 0-2 sphere normal U, 3-5 horizontal
-// direction of the current azimuth, 6 elevation accumulator, 7 sector sum,
-// 8 SVF sum; integers: domain, cell, azimuth, phase, upward steps, lattice
-// index m, work position; FP32 ray origin hi and lo). North and east are read
-// from the cell frame table at each new azimuth. Given the
-// result of the cell's last ray (or, in phase kPhaseStart, the work id k_new
-// of a new cell), it continues the bracket, or closes the azimuth (clip,
-// sector mean, SVF) and starts the next one, or finishes the cell. Returns 1
-// with the next ray's direction, 0 when the cell has finished (the state is
-// back in kPhaseStart and needs a new work id), -1 when k_new is past the
-// last work id.
+// Domain of search item k (doms sorted by item_begin).
+__device__ __forceinline__ int domain_of_item(const DomainDesc* __restrict__ doms, int ndom,
+                                              long long k) {
+  int lo = 0, hi = ndom - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (doms[mid].item_begin <= k) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// One step of a search item's bracketing search (mo_lradtopo_horayzon.cpp:
+// 490-555, 694-754) on the state `st` (FP64: 0-2 sphere normal U, 3-5
+// horizontal direction of the current azimuth, 6 elevation accumulator, 7
+// sector sum, 8 SVF sum; integers: domain, cell, azimuth, phase, upward
+// steps, lattice index m, work position, end azimuth of the item; FP32 ray
+// origin hi and lo). An item is one cell's run over one group of
+// consecutive azimuths: all L azimuths (the reference's chain) or, with the
+// learned start split into G groups, L / G of them starting at the MLP's
+// proposal. Items of a domain are numbered group-major (item = q * cells +
+// p), so the 32 items a warp takes are neighbouring cells in the same group.
+// North and east are read from the cell frame table at each new azimuth.
+// Given the result of the item's last ray (or, in phase kPhaseStart, the
+// item number k_new of a new item), it continues the bracket, or closes the
+// azimuth (clip, sector mean, SVF) and starts the next one, or finishes the
+// item. Returns 1 with the next ray's direction, 0 when the item has
+// finished (the state is back in kPhaseStart and needs a new item), -1 when
+// k_new is past the last item.
 template <bool kPrecise, class S>
 __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __restrict__ doms,
                                            int ndom, const int* __restrict__ order, int total,
@@ -634,12 +651,13 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
         alive = false;
         break;
       }
-      const long long g = order[k];
-      dom = domain_of(doms, ndom, g);
+      dom = domain_of_item(doms, ndom, k);
       const DomainDesc& D = doms[dom];
-      cell = (int)(g - D.cell_offset);
+      const long long local = k - D.item_begin;
+      const int grp = (int)(local / D.ncell_traced);
       // Cell frame (mo_lradtopo_horayzon.cpp:694-720) from k_cell_frames.
-      p = (int)(k - D.k_begin);
+      p = (int)(local - (long long)grp * D.ncell_traced);
+      cell = (int)(order[D.k_begin + p] - D.cell_offset);
       const long long nc = D.ncell;
       const double* fr = D.cell_frame + p;
       SV(0) = fr[0]; SV(1) = fr[nc]; SV(2) = fr[2 * nc];
@@ -652,9 +670,14 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
         SO(4) = org[4 * nc];
         SO(5) = org[5 * nc];
       }
-      SV(6) = 0.0; SV(7) = 0.0; SV(8) = 0.0;
-      a = 0;
-      m = 0;
+      SV(7) = 0.0; SV(8) = 0.0;
+      const int span = D.L / D.groups;
+      a = grp * span;
+      st.i(7) = a + span;  // end azimuth of the item
+      // The first elevation: the reference's 0 (cpp:511), or the learned
+      // proposal of the item's first azimuth.
+      m = D.start_m ? D.start_m[(long long)a * D.ncell + cell] : 0;
+      SV(6) = (double)m * D.two_ha;
       phase = kPhaseFirst;
     } else {
       // Result of the last ray: continue the bracket or close the azimuth.
@@ -700,12 +723,17 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       double svf = SV(8);
       if (D.refine != 1) svf = svf + lattice_svf_term(D, h, j);
       a++;
-      if (a == D.L) {
-        if (D.refine != 1) D.skyview[cell] = svf;  // divided by L in k_finish_outputs
+      if (a == st.i(7)) {
+        // Divided by L in k_finish_outputs; a split cell's groups leave
+        // partial sums, added there in group order.
+        if (D.refine != 1) {
+          if (D.groups == 1) D.skyview[cell] = svf;
+          else D.svf_part[(long long)(a / (D.L / D.groups) - 1) * D.ncell + cell] = svf;
+        }
         if (D.done) {
-          // Completion time of the domain's last cell (batch latency).
-          const unsigned long long fin_cells = atomicAdd(&D.done[0], 1ull) + 1ull;
-          if (fin_cells == (unsigned long long)D.ncell_traced) {
+          // Completion time of the domain's last item (batch latency).
+          const unsigned long long fin_items = atomicAdd(&D.done[0], 1ull) + 1ull;
+          if (fin_items == (unsigned long long)D.ncell_traced * (unsigned long long)D.groups) {
             unsigned long long now;
             asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
             D.done[1] = now;
@@ -719,10 +747,11 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       SV(8) = svf;
       phase = kPhaseFirst;
     }
-    // New azimuth: the elevation carries over (cpp:511), or starts at the
-    // learned proposal; horizontal direction cos(theta_a) N + sin(theta_a) E.
+    // New azimuth: the elevation carries over (cpp:511), or, with the
+    // learned start at every azimuth, starts at the proposal; horizontal
+    // direction cos(theta_a) N + sin(theta_a) E.
     const int16_t* start_m = doms[dom].start_m;
-    if (start_m && (a == 0 || doms[dom].start_all)) {
+    if (start_m && doms[dom].start_all) {
       m = start_m[(long long)a * doms[dom].ncell + cell];
       SV(6) = (double)m * doms[dom].two_ha;
     }
@@ -778,14 +807,14 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     k_trace_warp(const DomainDesc* __restrict__ doms, int ndom, const int* __restrict__ order,
                  int total, int* __restrict__ work, unsigned long long* __restrict__ counters,
                  int* __restrict__ err, int advance_min, int leaf_min, int chunk) {
-  // Per-lane search state (112 bytes; the rest of the SM's L1 caches the
+  // Per-lane search state (116 bytes; the rest of the SM's L1 caches the
   // tree). FP64: 0-2 sphere normal U, 3-5 horizontal direction of the
   // current azimuth, 6 elevation accumulator, 7 sector sum, 8 SVF sum.
   // Integers: domain, cell, azimuth, phase, upward steps, lattice index m of
-  // the current elevation, position of the cell in the work order. FP32 ray
-  // origin (hi, and lo in precise mode).
+  // the current elevation, position of the cell in the work order, end
+  // azimuth of the item. FP32 ray origin (hi, and lo in precise mode).
   __shared__ double sv[9][kFlatBlock];
-  __shared__ int si[7][kFlatBlock];
+  __shared__ int si[8][kFlatBlock];
   __shared__ float so[kPrecise ? 6 : 3][kFlatBlock];
   __shared__ int wq[2][kFlatBlock / 32];  // per warp: next and end of its chunk of work ids
   constexpr unsigned kFull = 0xffffffffu;
@@ -796,7 +825,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   }
   __syncwarp();
 #pragma unroll
-  for (int q = 0; q < 7; q++) si[q][t] = 0;
+  for (int q = 0; q < 8; q++) si[q][t] = 0;
   si[3][t] = kPhaseStart;
 
   bool alive = true, need = true, last_hit = false;
@@ -1122,7 +1151,15 @@ __device__ __forceinline__ void finish_cell(const DomainDesc& D, int cell) {
       }
     }
   }
-  D.skyview[cell] = (kRefine1 ? svf : D.skyview[cell]) / (double)D.L;
+  if (!kRefine1) {
+    if (D.groups == 1) {
+      svf = D.skyview[cell];
+    } else {
+      svf = D.svf_part[cell];
+      for (int q = 1; q < D.groups; q++) svf = svf + D.svf_part[(long long)q * nc + cell];
+    }
+  }
+  D.skyview[cell] = svf / (double)D.L;
 }
 
 __global__ void k_finish_outputs(const DomainDesc* __restrict__ doms, int ndom, int total) {
@@ -1335,14 +1372,14 @@ static cudaError_t launch_search(const DomainDesc* doms, int ndom, const int32_t
                                  cudaStream_t s);
 
 cudaError_t trace_flat(const DomainDesc* doms, int ndom, const int32_t* order, int total,
-                       int* work, unsigned long long* counters, int* err, const TraceKnobs& k,
-                       bool count_work, bool precise, cudaStream_t s) {
+                       int total_items, int* work, unsigned long long* counters, int* err,
+                       const TraceKnobs& k, bool count_work, bool precise, cudaStream_t s) {
   if (total <= 0 || ndom <= 0) return cudaSuccess;
   if (precise) k_cell_frames<true><<<grid_for(total, 256), 256, 0, s>>>(doms, ndom, order, total);
   else k_cell_frames<false><<<grid_for(total, 256), 256, 0, s>>>(doms, ndom, order, total);
   note_launches(1);
-  cudaError_t e =
-      launch_search(doms, ndom, order, total, work, counters, err, k, count_work, precise, s);
+  cudaError_t e = launch_search(doms, ndom, order, total_items, work, counters, err, k,
+                                count_work, precise, s);
   if (e != cudaSuccess) return e;
   k_finish_outputs<<<grid_for(total, 256), 256, 0, s>>>(doms, ndom, total);
   note_launches(1);

@@ -92,7 +92,7 @@ def _check_args(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_t
 def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
              advance_min=0, precision=0, mlp_params=None, raw_index=None, features=None,
              mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0,
-             direct_launch=False):
+             direct_launch=False, mlp_azimuth_groups=0):
     begin, count = (0, 0) if cells is None else (int(cells[0]), int(cells[1]) - int(cells[0]))
     opt = _lib.default_options(device=int(device), count_work=int(bool(count_work)),
                                elev_floor_deg=float(elev_floor_deg),
@@ -110,6 +110,7 @@ def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
         opt._keep = p  # alive for the duration of the call
         opt.mlp_params = p.ctypes.data
         opt.mlp_every_azimuth = int(bool(mlp_every_azimuth))
+        opt.mlp_azimuth_groups = int(mlp_azimuth_groups)
     if raw_index is not None:
         opt.raw_index = raw_index.data_ptr()
     if features is not None:
@@ -123,7 +124,7 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
                         verbose=False, return_stats=False, cells=None, kernel=0,
                         advance_min=0, precision=0, mlp_params=None,
                         mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0,
-                        direct_launch=False):
+                        direct_launch=False, mlp_azimuth_groups=0):
     """Compute the terrain horizon and sky view factor on the GPU.
 
     Arguments and returns as horizon_svf.pyx:15-76: FP64 1-D ``clon, clat``
@@ -136,7 +137,9 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
     persistent search on the binary BVH), its ``advance_min`` / ``leaf_min``
     knobs, the work-queue ``queue_chunk``, the BVH ``leaf_size``,
     ``direct_launch`` (launch each kernel directly instead of replaying the
-    captured CUDA graph of the BVH build and search) and, with
+    captured CUDA graph of the BVH build and search), the learned warm start
+    (``mlp_params``; ``mlp_every_azimuth``; ``mlp_azimuth_groups``: search
+    items per cell, -1 = chosen by the library, see hz_options) and, with
     ``return_stats``, a third return value with ray counts and phase times.
     """
     clon = _typed("clon", clon, np.float64, 1)
@@ -165,7 +168,7 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
     opt = _options(device, count_work, elev_floor_deg, verbose, cells, kernel, advance_min,
                    precision, mlp_params, mlp_every_azimuth=mlp_every_azimuth,
                    leaf_min=leaf_min, leaf_size=leaf_size, queue_chunk=queue_chunk,
-                   direct_launch=direct_launch)
+                   direct_launch=direct_launch, mlp_azimuth_groups=mlp_azimuth_groups)
     st = _lib.Stats()
     rc = L.hz_horizon_svf(clon.ctypes.data_as(_D), clat.ctypes.data_as(_D),
                           hsurf.ctypes.data_as(_D), vlon.ctypes.data_as(_D),
@@ -186,7 +189,8 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
                             count_work=False, elev_floor_deg=-85.0, cells=None, kernel=0,
                             advance_min=0, precision=0, mlp_params=None, raw_index=None,
                             features=None, mlp_every_azimuth=False, leaf_min=0,
-                            leaf_size=0, queue_chunk=0, direct_launch=False):
+                            leaf_size=0, queue_chunk=0, direct_launch=False,
+                            mlp_azimuth_groups=0):
     """Same computation on CUDA tensors (torch) already resident on one GPU.
 
     Inputs: contiguous float64 / int32 tensors on the same device, layouts as
@@ -224,7 +228,7 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
     opt = _options(dev.index if dev.index is not None else -1, count_work,
                    elev_floor_deg, False, cells, kernel, advance_min, precision, mlp_params,
                    raw_index, features, mlp_every_azimuth, leaf_min, leaf_size, queue_chunk,
-                   direct_launch)
+                   direct_launch, mlp_azimuth_groups)
     st = _lib.Stats()
     rc = L.hz_horizon_svf_device(clon.data_ptr(), clat.data_ptr(), hsurf.data_ptr(),
                                  vlon.data_ptr(), vlat.data_ptr(),
@@ -300,7 +304,7 @@ def mesh_enu32(clon, clat, hsurf, vlon, vlat, cells_of_vertex, grid_type, device
 def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_deg=-85.0,
                            advance_min=0, return_stats=False, precision=0, mlp_params=None,
                            mlp_every_azimuth=False, kernel=0, leaf_min=0, leaf_size=0,
-                           queue_chunk=0, direct_launch=False):
+                           queue_chunk=0, direct_launch=False, mlp_azimuth_groups=0):
     """Many independent domains in one call (one persistent search launch).
 
     ``domains``: sequence of ``(inputs, args)`` with ``inputs`` the six arrays
@@ -329,7 +333,7 @@ def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_d
     opt = _options(device, count_work, elev_floor_deg, False, None, kernel, advance_min,
                    precision, mlp_params, mlp_every_azimuth=mlp_every_azimuth,
                    leaf_min=leaf_min, leaf_size=leaf_size, queue_chunk=queue_chunk,
-                   direct_launch=direct_launch)
+                   direct_launch=direct_launch, mlp_azimuth_groups=mlp_azimuth_groups)
     st = _lib.Stats()
     rc = _lib.load().hz_horizon_svf_batch(arr, len(structs), 0, None, C.byref(opt),
                                           C.byref(st))

@@ -77,6 +77,15 @@ typedef struct hz_options {
                                 warp takes from the work queue at a time (0 = 32) */
     int32_t direct_launch;   /* 1: launch every kernel directly instead of replaying a
                                 captured CUDA graph of the BVH build and search */
+    /* Learned warm start: search items per cell. 0 or 1: one item runs the
+       cell's azimuths as the reference's chain, the MLP's proposal starting
+       the first one. G > 1 (a divisor of num_hori): G items of num_hori / G
+       sectors each, every item starting at the proposal of its first
+       azimuth, so that one cell's azimuths run on G lanes at once (small
+       domains fill the GPU). -1: the library picks G per domain, the
+       smallest divisor of num_hori that gives the call at least four search
+       items per resident GPU thread (1 for domains that fill the GPU). */
+    int32_t mlp_azimuth_groups;
 } hz_options;
 
 enum {

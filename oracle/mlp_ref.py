@@ -3,8 +3,14 @@
 TEST INFRASTRUCTURE: the checker of the GPU training kernels' gradients
 (tests/). Parameter layout as hz_mlp_train_step: W1[32][64], b1[64],
 W2[64][64], b2[64], W3[64], b3; ReLU hidden layers; loss = mean((y - t)^2).
-The GPU forward rounds the weights to BF16 first; pass the same rounded
-values here.
+
+``forward`` / ``loss_and_grad`` are the exact network in FP64.
+``forward_bf16`` / ``loss_and_grad_bf16`` restate the GPU kernels' mixed
+precision (csrc/hz_learn.cu): weights and biases rounded to BF16 (pass
+``bf16_round(p)``), the inputs X and the first hidden layer's activations
+rounded to BF16 before their products, and in the backward pass G2 =
+dL/da2 and G1 = dL/da1 rounded to BF16 before the products G2 W2^T, H1^T G2
+and X^T G1; every sum is taken in FP64 here (FP32 on the GPU).
 """
 import numpy as np
 
@@ -60,5 +66,44 @@ def loss_and_grad(p, X, T):
     g1 = (g2 @ W2.T) * (a1 > 0)
     gW1 = X.T @ g1
     gb1 = g1.sum(0)
+    grad = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3, [gb3]])
+    return loss, grad
+
+
+def _bf16_64(x):
+    """BF16 rounding of FP64 values through FP32, as the GPU rounds its FP32
+    intermediates."""
+    return bf16_round(np.asarray(x, dtype=np.float64).astype(np.float32)).astype(np.float64)
+
+
+def forward_bf16(p, X):
+    """The GPU forward pass: y and the intermediates (Xb, a1, h1b, a2, h2)."""
+    W1, b1, W2, b2, W3, b3 = unpack(p)
+    Xb = _bf16_64(X)
+    a1 = Xb @ W1 + b1
+    h1b = _bf16_64(np.maximum(a1, 0.0))
+    a2 = h1b @ W2 + b2
+    h2 = np.maximum(a2, 0.0)
+    y = h2 @ W3 + b3
+    return y, (Xb, a1, h1b, a2, h2)
+
+
+def loss_and_grad_bf16(p, X, T):
+    """Mean squared error and the gradient the GPU training kernel computes."""
+    W1, b1, W2, b2, W3, b3 = unpack(p)
+    y, (Xb, a1, h1b, a2, h2) = forward_bf16(p, X)
+    n = Xb.shape[0]
+    d = y - np.asarray(T, dtype=np.float64)
+    loss = np.mean(d * d)
+    g = 2.0 * d / n
+    gW3 = h2.T @ g
+    gb3 = g.sum()
+    G2 = np.outer(g, W3) * (a2 > 0)
+    gb2 = G2.sum(0)
+    G2b = _bf16_64(G2)
+    gW2 = h1b.T @ G2b
+    G1 = (G2b @ W2.T) * (h1b > 0)
+    gb1 = G1.sum(0)
+    gW1 = Xb.T @ _bf16_64(G1)
     grad = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3, [gb3]])
     return loss, grad

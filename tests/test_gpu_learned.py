@@ -24,25 +24,53 @@ def _batch(torch, n, seed):
     return X, T, torch.from_numpy(X).to(dev), torch.from_numpy(T).to(dev)
 
 
+# The tensor-core kernels round X and h1 to BF16 after FP32 sums; the FP64
+# oracle rounds the same values after FP64 sums, so a value within FP32
+# rounding of a BF16 rounding boundary can round the other way (one BF16
+# ulp, 2^-8 relative, of one hidden unit). Forward bar: 97 % of the outputs
+# within 1e-4 (relative 1e-4), all within 5e-3.
+def _assert_forward_close(y, y_ref):
+    d = np.abs(y - y_ref)
+    assert np.mean(d <= 1e-4 + 1e-4 * np.abs(y_ref)) >= 0.97, np.sort(d)[-10:]
+    assert d.max() <= 5e-3, d.max()
+
+
 def test_mlp_forward_and_gradients_match_fp64_oracle(torch):
+    """Forward pass, loss and gradient of the BF16 tensor-core kernels
+    against the FP64 restatement of the same rounding points."""
     p = mlp_ref.bf16_round(learned.init_params(3) + 0.01)
     X, T, Xd, Td = _batch(torch, 700, 1)
-    y_ref, _ = mlp_ref.forward(p, X)
+    y_ref, _ = mlp_ref.forward_bf16(p, X)
     y = learned.forward(p, Xd).cpu().numpy()
-    np.testing.assert_allclose(y, y_ref, rtol=1e-4, atol=1e-4)
-    loss_ref, g_ref = mlp_ref.loss_and_grad(p, X, T)
+    _assert_forward_close(y, y_ref)
+    loss_ref, g_ref = mlp_ref.loss_and_grad_bf16(p, X, T)
     loss, g = learned.gradients(p, Xd, Td)
     assert abs(loss - loss_ref) <= 1e-4 * max(1.0, loss_ref)
     scale = np.abs(g_ref).max()
-    np.testing.assert_allclose(g, g_ref, rtol=2e-3, atol=1e-5 * scale)
+    np.testing.assert_allclose(g, g_ref, rtol=2e-3, atol=1e-4 * scale)
+    # And against the exact FP64 network: within BF16 precision.
+    _, g_exact = mlp_ref.loss_and_grad(p, X, T)
+    assert np.linalg.norm(g - g_exact) <= 0.03 * np.linalg.norm(g_exact)
+
+
+def test_mlp_gradients_over_many_chunks(torch):
+    """A batch of several thousand samples (many 64-sample chunks per block,
+    a ragged last chunk): the per-block accumulators and their reductions."""
+    p = mlp_ref.bf16_round(learned.init_params(4) - 0.02)
+    X, T, Xd, Td = _batch(torch, 40001, 7)
+    loss_ref, g_ref = mlp_ref.loss_and_grad_bf16(p, X, T)
+    loss, g = learned.gradients(p, Xd, Td)
+    assert abs(loss - loss_ref) <= 1e-4 * max(1.0, loss_ref)
+    scale = np.abs(g_ref).max()
+    np.testing.assert_allclose(g, g_ref, rtol=2e-3, atol=1e-4 * scale)
 
 
 def test_mlp_weights_are_rounded_to_bf16(torch):
     p = learned.init_params(5)
     X, _, Xd, _ = _batch(torch, 64, 2)
     y = learned.forward(p, Xd).cpu().numpy()
-    y_bf, _ = mlp_ref.forward(mlp_ref.bf16_round(p), X)
-    np.testing.assert_allclose(y, y_bf, rtol=1e-4, atol=1e-4)
+    y_bf, _ = mlp_ref.forward_bf16(mlp_ref.bf16_round(p), X)
+    _assert_forward_close(y, y_bf)
 
 
 def test_training_reduces_loss(torch):
@@ -98,7 +126,7 @@ def test_learned_start_keeps_results_and_saves_rays(trained):
           "SVF 1e-3):", stats)
     for k in ("learned", "untrained"):  # first azimuth from the MLP, then chained
         assert stats[k][0] >= 0.999 and stats[k][1] >= 0.999, stats
-    assert stats["every"][0] >= 0.995, stats  # every azimuth restarted: more exposure
+    assert stats["every"][0] >= 0.999, stats  # every azimuth restarted: more exposure
     # Reference frame: the parity bar on the horizons.
     hr0, _ = horizon_svf_comp_py(*d.inputs(), *args)
     hr1, _ = horizon_svf_comp_py(*d.inputs(), *args, mlp_params=p)
@@ -125,3 +153,65 @@ def test_learned_start_in_a_batch_equals_single_calls(trained):
         h1, s1 = horizon_svf_comp_py(*d.inputs(), *a, mlp_params=p)
         np.testing.assert_array_equal(h, h1)
         np.testing.assert_array_equal(s, s1)
+
+
+def test_split_items_equal_every_azimuth_restarts(trained):
+    """One search item per (cell, azimuth) starting at the proposal (groups
+    = num_hori) casts exactly the rays of the every-azimuth mode, which
+    restarts each azimuth of the chain at its proposal: same results, same
+    ray count. The library's own choice (-1) on a small domain is that
+    split."""
+    p, kw, args = trained
+    d = synthetic.make_domain(seed=10, **kw)
+    loc = dict(mlp_params=p, return_stats=True)
+    he, se, ste = horizon_svf_comp_py(*d.inputs(), *args, mlp_every_azimuth=True, **loc)
+    hs, ss, sts = horizon_svf_comp_py(*d.inputs(), *args, mlp_azimuth_groups=args[0], **loc)
+    np.testing.assert_array_equal(hs, he)
+    np.testing.assert_allclose(ss, se, rtol=0, atol=1e-12)
+    assert sts["num_rays"] == ste["num_rays"]
+    ha, sa = horizon_svf_comp_py(*d.inputs(), *args, mlp_params=p, mlp_azimuth_groups=-1)
+    np.testing.assert_array_equal(ha, hs)
+
+
+@pytest.mark.parametrize("groups,args", [
+    (4, (24, 1, 8000.0, 0.2, 1, 2)),
+    (8, (24, 1, 8000.0, 0.2, 1, 0)),
+    (6, (12, 1, 6000.0, 0.3, 3, 1)),   # refine 3: per-group SVF sums
+    (12, (12, 0, 6000.0, 0.2, 2, 2)),  # grid_type 0, refine 2
+])
+def test_split_items_match_the_oracle(trained, groups, args):
+    """Azimuth groups, each starting at the learned proposal: the parity bar
+    against the CPU oracle (|dhorizon| <= 0.25 deg on >= 99.9 %, |dSVF| <=
+    1e-3), including refine_factor > 1, where each group leaves a partial
+    SVF sum that the epilogue adds in group order."""
+    from oracle import api as oracle
+    p, kw, _ = trained
+    d = synthetic.make_domain(seed=11, **kw)
+    h, s, st = horizon_svf_comp_py(*d.inputs(), *args, mlp_params=p, mlp_azimuth_groups=groups,
+                                   precision=1, return_stats=True)
+    ho, so, _ = oracle.horizon_svf(*d.inputs(), *args, precision=1)
+    dh = np.abs(h - ho)
+    assert np.mean(dh <= 0.25) >= 0.999, np.mean(dh <= 0.25)
+    assert np.abs(s - so).max() <= 1e-3
+    evals = d.ncell * args[0] * args[4]
+    assert st["num_rays"] >= 2 * evals - 1e-9  # a hit and a miss per traced azimuth
+
+
+def test_split_items_in_a_batch_equal_single_calls(trained):
+    from horayzon_extpar_gb300.horizon_svf import horizon_svf_comp_batch
+    p, kw, args = trained
+    doms = [synthetic.make_domain(seed=s, **kw) for s in (12, 13)]
+    args2 = (16, 1, 6000.0, 0.2, 2, 1)
+    outs = horizon_svf_comp_batch([(doms[0].inputs(), args), (doms[1].inputs(), args2)],
+                                  mlp_params=p, mlp_azimuth_groups=4)
+    for d, a, (h, s) in zip(doms, (args, args2), outs):
+        h1, s1 = horizon_svf_comp_py(*d.inputs(), *a, mlp_params=p, mlp_azimuth_groups=4)
+        np.testing.assert_array_equal(h, h1)
+        np.testing.assert_array_equal(s, s1)
+
+
+def test_split_groups_must_divide_num_hori(trained):
+    p, kw, args = trained
+    d = synthetic.make_domain(seed=14, **kw)
+    with pytest.raises(ValueError, match="does not divide"):
+        horizon_svf_comp_py(*d.inputs(), *args, mlp_params=p, mlp_azimuth_groups=5)

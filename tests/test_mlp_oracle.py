@@ -37,3 +37,24 @@ def test_mlp_params_save_load_round_trip(tmp_path):
     np.testing.assert_array_equal(learned.load_params(path), p)
     with pytest.raises(ValueError):
         learned.save_params(path, p[:10])
+
+
+def test_mixed_precision_oracle_is_close_to_the_exact_network():
+    """The BF16 restatement of the GPU arithmetic differs from the exact
+    FP64 network only by BF16 rounding (relative 2^-8 per rounded value)."""
+    rng = np.random.default_rng(1)
+    p = mlp_ref.bf16_round(rng.normal(0, 0.2, mlp_ref.N_PARAMS)).astype(np.float64)
+    X = rng.normal(0, 1, (300, 32))
+    T = rng.normal(0, 1, 300)
+    y, _ = mlp_ref.forward(p, X)
+    yb, _ = mlp_ref.forward_bf16(p, X)
+    assert np.abs(yb - y).max() <= 0.03 * np.abs(y).max()
+    l, g = mlp_ref.loss_and_grad(p, X, T)
+    lb, gb = mlp_ref.loss_and_grad_bf16(p, X, T)
+    assert abs(lb - l) <= 0.02 * l
+    assert np.linalg.norm(gb - g) <= 0.03 * np.linalg.norm(g)
+    # Inputs and activations already on the BF16 grid: the restatement's
+    # forward pass is the exact one.
+    Xq = mlp_ref.bf16_round(X).astype(np.float64)
+    _, (Xb, _, _, _, _) = mlp_ref.forward_bf16(p, Xq)
+    np.testing.assert_array_equal(Xb, Xq)
