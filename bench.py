@@ -724,6 +724,66 @@ def run_gpu(args):
     return 0
 
 
+def run_sharded(args):
+    """One benchmark domain over the N ranks (strong scaling): every rank
+    builds the mesh and BVH and traces its contiguous cell range
+    (shard.horizon_svf_sharded); a step ends with the all-gather of the
+    slices. Timed with CUDA events on each rank (max over ranks), like the
+    replica mode."""
+    import torch
+    import torch.distributed as dist
+
+    from horayzon_extpar_gb300 import _lib, shard
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    else:
+        dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % _free_port(),
+                                rank=0, world_size=1)
+    dev = torch.device("cuda", local)
+    _lib.load(build_if_missing=True)
+    dom = make_workload(0, args.box_km)
+    evals = dom.ncell * ARGS[0]
+    host = [np.ascontiguousarray(a) for a in dom.inputs()]
+    for _ in range(args.warmup):
+        shard.horizon_svf_sharded(*host, *ARGS, device=dev)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        shard.horizon_svf_sharded(*host, *ARGS, device=dev)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    sec = (time.perf_counter() - t0) / args.steps
+    t = torch.tensor([sec], dtype=torch.float64, device=dev if world > 1 else "cpu")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    sec = float(t[0])
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": evals / sec, "unit": "evals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
+            "dtype": "f32 rays / f64 frames", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "ncell": dom.ncell,
+                       "parallelism": "cell-range shards of one domain over %d ranks" % world,
+                       "timing": "host wall clock per step: H2D of the domain, mesh + BVH, "
+                                 "the rank's cell range, all-gather"}}), flush=True)
+    dist.destroy_process_group()
+    return 0
+
+
+def _free_port():
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -740,9 +800,14 @@ def main():
     ap.add_argument("--parity-cells", type=int, default=20000,
                     help="cells of the oracle sample each configuration is compared on "
                          "(the main workload uses the CPU baseline's sample)")
+    ap.add_argument("--mode", choices=["replica", "sharded"], default="replica",
+                    help="replica: one independent domain per rank (weak scaling, the "
+                         "default line); sharded: one domain's cells split over the ranks")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "sharded":
+        return run_sharded(args)
     return run_gpu(args)
 
 

@@ -49,7 +49,8 @@ class Options(C.Structure):
                 ("mlp_every_azimuth", C.c_int32), ("raw_index", C.c_void_p),
                 ("features", C.c_void_p), ("leaf_min", C.c_int32),
                 ("leaf_size", C.c_int32), ("queue_chunk", C.c_int32),
-                ("direct_launch", C.c_int32), ("mlp_azimuth_groups", C.c_int32)]
+                ("direct_launch", C.c_int32), ("mlp_azimuth_groups", C.c_int32),
+                ("start_index", C.c_void_p)]
 
 
 HZ_KERNEL_PERSISTENT, HZ_KERNEL_PER_CELL, HZ_KERNEL_PERSISTENT_BVH2 = 0, 1, 2

@@ -132,6 +132,8 @@ struct Buffers {
   // BVH
   Node* nodes;
   Node4* nodes4;     // wide traversal only
+  Node4* top4;       // wide traversal: copies of the top nodes (shared-memory staging)
+  int* n_top;
   Tri* tris;
   BvhScratch bvh;
   // search
@@ -183,7 +185,11 @@ Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhor
   b.cell_origin = c.take<float>(6 * ncell);
   const long long nt = max_tri > 0 ? max_tri : 1;
   b.nodes = c.take<Node>(nt > 1 ? nt - 1 : 1);
-  if (wide) b.nodes4 = c.take<Node4>(nt > 1 ? nt - 1 : 1);
+  if (wide) {
+    b.nodes4 = c.take<Node4>(nt > 1 ? nt - 1 : 1);
+    b.top4 = c.take<Node4>(kTopNodesLarge);
+    b.n_top = c.take<int>(4);
+  }
   b.tris = c.take<Tri>(nt);
   if (precise) {
     b.vert_lo = c.take<float>(3 * max_mv);
@@ -458,8 +464,20 @@ struct RunOut {
 // Runs the pipeline for n domains whose arrays are device pointers in pr[].
 // With stop != kFull it ends after the mesh (or ENU) stage and leaves the
 // results in b[].
+// Top nodes of the 4-wide tree staged in shared memory by the search
+// (single-domain calls): HZ_TOP_NODES = 0 (none), 21 or 85.
+int top_nodes_setting() {
+  static const int v = [] {
+    const char* e = getenv("HZ_TOP_NODES");
+    const int x = e ? atoi(e) : 0;
+    return x >= kTopNodesLarge ? kTopNodesLarge : (x >= kTopNodesSmall ? kTopNodesSmall : 0);
+  }();
+  return v;
+}
+
 int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const BatchBuffers& bb,
               cudaStream_t s, const hz_options& opt, hz_stats* st, Stop stop, RunOut* out) {
+  const int top_nodes = opt.kernel == HZ_KERNEL_PERSISTENT ? top_nodes_setting() : 0;
   g_launches = 0;
   g_log.clear();
   out->n_tri.assign(n, 0);
@@ -586,9 +604,14 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   {
     Fork fk(E, s, n);
     HZ_CUDA(fk.begin());
-    for (int d = 0; d < n; d++)
+    for (int d = 0; d < n; d++) {
       HZ_CUDA(bvh_build(b[d].vert32, b[d].vot, out->n_tri[d], b[d].nodes, b[d].tris, b[d].bvh,
                         fk.on(d), b[d].vert_lo, b[d].tri_lo, b[d].nodes4, opt.leaf_size));
+      if (n == 1 && b[d].nodes4 && top_nodes > 0)
+        HZ_CUDA(bvh_stage_top4(b[d].nodes4, out->n_tri[d],
+                               top_nodes >= kTopNodesLarge ? 4 : 3, b[d].top4, b[d].n_top,
+                               fk.on(d)));
+    }
     HZ_CUDA(fk.end());
   }
   HZ_CUDA(cap.record(E.ev[2]));
@@ -739,11 +762,13 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.elev_cs = b[d].elev_cs;
       D.svf_lattice = b[d].svf_lattice;
       D.done = n > 1 ? bb.done + 2 * d : nullptr;
-      D.start_m = opt.mlp_params ? b[d].start_m : nullptr;
+      D.start_m = opt.mlp_params ? b[d].start_m : opt.start_index;
       D.start_all = opt.mlp_every_azimuth ? 1 : 0;
       D.groups = P.groups;
       D.item_begin = total_items;
       D.svf_part = b[d].svf_part;
+      D.top4 = n == 1 && top_nodes > 0 ? b[d].top4 : nullptr;
+      D.n_top = b[d].n_top;
       D.raw_j = n == 1 ? opt.raw_index : nullptr;
       D.centre = frames[d].centre;
       D.pole = frames[d].pole;
@@ -778,7 +803,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     k_stamp<<<1, 1, 0, s>>>(bb.t0);
     note_launches(1);
     HZ_CUDA(cudaGetLastError());
-    const TraceKnobs knobs{adv, leaf, opt.queue_chunk, variant};
+    const TraceKnobs knobs{adv, leaf, opt.queue_chunk, variant, n == 1 ? top_nodes : 0};
     HZ_CUDA(trace_flat(bb.doms, n, bb.order, (int)total, (int)total_items, bb.work,
                        bb.counters, bb.err, knobs, opt.count_work != 0,
                        b[0].tri_lo != nullptr, s));
@@ -947,7 +972,9 @@ constexpr int kItemsPerLane = 4;
 int azimuth_groups(const hz_domain* doms, int n, const hz_options& opt, int* groups) {
   for (int d = 0; d < n; d++) groups[d] = 1;
   const int G = opt.mlp_azimuth_groups;
-  if (opt.mlp_params == nullptr || opt.mlp_every_azimuth || G == 0 || G == 1) return HZ_OK;
+  if ((opt.mlp_params == nullptr && opt.start_index == nullptr) || opt.mlp_every_azimuth ||
+      G == 0 || G == 1)
+    return HZ_OK;
   if (G > 1) {
     for (int d = 0; d < n; d++) {
       if (doms[d].num_hori % G != 0)
@@ -1017,6 +1044,9 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
   const bool wide = opt.kernel != HZ_KERNEL_PER_CELL && trace_variant(opt) == kTraceWide;
   if ((opt.raw_index || opt.features) && (n != 1 || !on_device))
     return fail(HZ_ERR_VALUE, "raw_index / features are outputs of the device entry point");
+  if (opt.start_index && (n != 1 || !on_device || opt.mlp_params))
+    return fail(HZ_ERR_VALUE, "start_index is an input of the device entry point (one domain, "
+                              "no mlp_params)");
   std::vector<int> groups(n, 1);
   rc = azimuth_groups(doms, n, opt, groups.data());
   if (rc) return rc;

@@ -279,7 +279,53 @@ __global__ void k_collapse4(const Node* __restrict__ nodes, int n_nodes,
   out[i] = q;
 }
 
+// Level-synchronous walk of the top levels of the 4-wide tree by one block:
+// copies each visited node into top4 and renames its children that are
+// copied too (next level) to kTopFlag | slot.
+__global__ void k_stage_top4(const Node4* __restrict__ nodes4, int levels,
+                             Node4* __restrict__ top4, int* __restrict__ n_top) {
+  __shared__ int queue[kTopNodesLarge];
+  __shared__ int count;
+  if (threadIdx.x == 0) {
+    queue[0] = 0;
+    count = 1;
+  }
+  __syncthreads();
+  int begin = 0, end = 1;
+  for (int level = 0; level < levels; level++) {
+    for (int i = begin + threadIdx.x; i < end; i += blockDim.x) {
+      Node4 nd = nodes4[queue[i]];
+      int ch[4] = {nd.child.x, nd.child.y, nd.child.z, nd.child.w};
+      if (level + 1 < levels) {
+        for (int j = 0; j < 4; j++) {
+          if (ch[j] < 0) continue;  // leaf or empty
+          const int slot = atomicAdd(&count, 1);  // < kTopNodesLarge for levels <= 4
+          queue[slot] = ch[j];
+          ch[j] = kTopFlag | slot;
+        }
+      }
+      nd.child = make_int4(ch[0], ch[1], ch[2], ch[3]);
+      top4[i] = nd;
+    }
+    __syncthreads();
+    begin = end;
+    end = count;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *n_top = begin;
+}
+
 }  // namespace
+
+cudaError_t bvh_stage_top4(const Node4* nodes4, int n_tri, int levels, Node4* top4, int* n_top,
+                           cudaStream_t s) {
+  if (levels < 1) levels = 1;
+  if (levels > 4) levels = 4;
+  if (n_tri <= 0) return cudaMemsetAsync(n_top, 0, sizeof(int), s);
+  k_stage_top4<<<1, 128, 0, s>>>(nodes4, levels, top4, n_top);
+  note_launches(1);
+  return cudaGetLastError();
+}
 
 size_t bvh_scratch_bytes(long long n) {
   if (n < 1) n = 1;

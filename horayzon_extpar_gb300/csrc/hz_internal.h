@@ -82,6 +82,12 @@ cudaError_t bvh_build(const float* vert32, const int* vot, int n_tri, Node* node
                       const float* vert_lo = nullptr, float4* tri_lo = nullptr,
                       Node4* nodes4 = nullptr, int leaf_max = kLeafMax);
 
+// Copies of the top `levels` levels (1..4) of the 4-wide tree (root 0) into
+// top4[<= kTopNodesLarge], child references between copied nodes rewritten to
+// kTopFlag | slot (slot 0 = the root); the node count goes to *n_top.
+cudaError_t bvh_stage_top4(const Node4* nodes4, int n_tri, int levels, Node4* top4, int* n_top,
+                           cudaStream_t s);
+
 // ---- hz_trace.cu ------------------------------------------------------------
 struct TraceParams {
   const double* cell_enu;   // [3 * ncell] FP64 ENU of cell centres
@@ -168,6 +174,8 @@ struct DomainDesc {
   int root, ncell, ncell_traced, nhori, refine, L, svf_type;
   int n_tri;                  // triangles of the tree (nodes: max(1, n_tri - 1))
   float tfar;
+  const Node4* top4;          // optional: copies of the tree's top nodes (bvh_stage_top4)
+  const int* n_top;           // device: nodes in top4
 };
 
 // Persistent flattened search (same rays and results as trace_exact) over
@@ -195,6 +203,8 @@ struct TraceKnobs {
   int leaf_min;     // 1..32
   int chunk;        // work ids a warp claims per atomic (< 1: kDefaultChunk)
   int variant;      // kTrace*
+  int top_nodes;    // 4-wide tree, single domain: top nodes staged in shared memory
+                    // (0, kTopNodesSmall or kTopNodesLarge; needs DomainDesc::top4)
 };
 // `total` traced cells (frames, epilogue) and `total_items` search items
 // (the sum of groups x traced cells over the domains).

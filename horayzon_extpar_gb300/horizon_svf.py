@@ -92,7 +92,7 @@ def _check_args(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_t
 def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
              advance_min=0, precision=0, mlp_params=None, raw_index=None, features=None,
              mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0,
-             direct_launch=False, mlp_azimuth_groups=0):
+             direct_launch=False, mlp_azimuth_groups=0, start_index=None):
     begin, count = (0, 0) if cells is None else (int(cells[0]), int(cells[1]) - int(cells[0]))
     opt = _lib.default_options(device=int(device), count_work=int(bool(count_work)),
                                elev_floor_deg=float(elev_floor_deg),
@@ -109,6 +109,10 @@ def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
                              % _lib.load().hz_mlp_num_params())
         opt._keep = p  # alive for the duration of the call
         opt.mlp_params = p.ctypes.data
+        opt.mlp_every_azimuth = int(bool(mlp_every_azimuth))
+        opt.mlp_azimuth_groups = int(mlp_azimuth_groups)
+    if start_index is not None:
+        opt.start_index = start_index.data_ptr()
         opt.mlp_every_azimuth = int(bool(mlp_every_azimuth))
         opt.mlp_azimuth_groups = int(mlp_azimuth_groups)
     if raw_index is not None:
@@ -190,15 +194,17 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
                             advance_min=0, precision=0, mlp_params=None, raw_index=None,
                             features=None, mlp_every_azimuth=False, leaf_min=0,
                             leaf_size=0, queue_chunk=0, direct_launch=False,
-                            mlp_azimuth_groups=0):
+                            mlp_azimuth_groups=0, start_index=None):
     """Same computation on CUDA tensors (torch) already resident on one GPU.
 
     Inputs: contiguous float64 / int32 tensors on the same device, layouts as
     in :func:`horizon_svf_comp_py`. ``horizon``/``skyview`` may be passed
     preallocated. ``cells=(begin, end)`` traces only that cell range (the
     mesh and BVH always cover the whole domain; other output entries are left
-    untouched). Runs on ``stream`` (default: torch's current stream) and
-    returns ``(horizon, skyview, stats)``.
+    untouched). ``start_index`` (int16 tensor [L, ncell] on the device):
+    given warm-start lattice indices used like the MLP's proposals (see
+    hz_options.start_index). Runs on ``stream`` (default: torch's current
+    stream) and returns ``(horizon, skyview, stats)``.
     """
     import torch
 
@@ -224,11 +230,17 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
         skyview = torch.empty(ncell, dtype=torch.float64, device=dev)
     if stream is None:
         stream = torch.cuda.current_stream(dev)
+    if start_index is not None:
+        Lz = int(num_hori) * int(refine_factor)
+        if (start_index.dtype != torch.int16 or start_index.device != dev
+                or not start_index.is_contiguous() or tuple(start_index.shape) != (Lz, ncell)):
+            raise ValueError("'start_index' must be a contiguous int16 tensor of shape "
+                             "(num_hori * refine_factor, ncell) on %s" % dev)
     L = _lib.load()
     opt = _options(dev.index if dev.index is not None else -1, count_work,
                    elev_floor_deg, False, cells, kernel, advance_min, precision, mlp_params,
                    raw_index, features, mlp_every_azimuth, leaf_min, leaf_size, queue_chunk,
-                   direct_launch, mlp_azimuth_groups)
+                   direct_launch, mlp_azimuth_groups, start_index)
     st = _lib.Stats()
     rc = L.hz_horizon_svf_device(clon.data_ptr(), clat.data_ptr(), hsurf.data_ptr(),
                                  vlon.data_ptr(), vlat.data_ptr(),

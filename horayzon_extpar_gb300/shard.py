@@ -7,6 +7,10 @@ ranges: every rank builds the whole mesh and BVH (cheap, no exchange) and
 traces only its range; the only collective is the final gather of the
 horizon/skyview slices and the sum of the ray counts. Independent domains
 (batches of regional grids) need no collective at all.
+
+``horizon_svf_sharded`` is that path end to end: each rank of a
+torch.distributed group calls the library's device entry point on its own
+GPU for its cell range, then the ranks all-gather the slices.
 """
 from __future__ import annotations
 
@@ -51,7 +55,7 @@ def gather(horizon_local, skyview_local, rays_local: int, ncell: int, num_hori: 
     world = dist.get_world_size(group)
     rank = dist.get_rank(group)
     ranges = cell_ranges(ncell, world)
-    width = max(e - b for b, e in ranges)
+    width = max(max(e - b for b, e in ranges), 1)
     dev = horizon_local.device if isinstance(horizon_local, torch.Tensor) else "cpu"
     buf = torch.full((num_hori + 1, width), float("nan"), dtype=torch.float64, device=dev)
     b, e = ranges[rank]
@@ -67,3 +71,62 @@ def gather(horizon_local, skyview_local, rays_local: int, ncell: int, num_hori: 
         parts.append((rb, re_, o[:num_hori, : re_ - rb], o[num_hori, : re_ - rb]))
     h, s = assemble(parts, ncell, num_hori)
     return h, s, int(rays.item())
+
+
+def horizon_svf_sharded(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_type,
+                        dist_search, ray_org_elev, refine_factor, svf_type, *, group=None,
+                        device=None, return_stats=False, **options):
+    """One domain over the ranks of a torch.distributed group.
+
+    Every rank passes the whole domain (the reference's arrays, numpy or
+    torch). Each rank copies it to its GPU (``device``, default
+    ``cuda:<LOCAL_RANK>``), builds the mesh and BVH there, and traces its
+    contiguous cell range (:func:`cell_ranges`) with
+    ``horizon_svf_comp_device(..., cells=(begin, end))``; then the slices are
+    all-gathered (on the GPU for an NCCL group, through host memory
+    otherwise) and every rank returns the full ``horizon`` (num_hori, ncell)
+    and ``skyview`` (ncell) as numpy arrays, bit-identical to a single call
+    on one GPU. ``options`` go to the device entry point (kernel knobs,
+    precision, learned start). With ``return_stats`` a third value holds the
+    total ray count and this rank's phase times.
+    """
+    import os
+
+    import torch
+    import torch.distributed as dist
+
+    from .horizon_svf import horizon_svf_comp_device
+
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    if device is None:
+        device = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device(device)
+
+    def on_dev(a, dtype):
+        t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a))
+        return t.to(device=dev, dtype=dtype).contiguous()
+
+    f64 = [on_dev(a, torch.float64) for a in (clon, clat, hsurf, vlon, vlat)]
+    cov = on_dev(cells_of_vertex, torch.int32)
+    ncell = f64[0].numel()
+    num_hori = int(num_hori)
+    b, e = cell_ranges(ncell, world)[rank]
+    horizon = torch.empty((num_hori, ncell), dtype=torch.float64, device=dev)
+    skyview = torch.empty(ncell, dtype=torch.float64, device=dev)
+    st = {"num_rays": 0}
+    if e > b:
+        _, _, st = horizon_svf_comp_device(*f64, cov, num_hori, grid_type, dist_search,
+                                           ray_org_elev, refine_factor, svf_type,
+                                           horizon=horizon, skyview=skyview, cells=(b, e),
+                                           **options)
+    h_loc, s_loc = horizon[:, b:e], skyview[b:e]
+    if dist.get_backend(group) != "nccl":
+        h_loc, s_loc = h_loc.cpu(), s_loc.cpu()
+    h, s, rays = gather(h_loc, s_loc, st["num_rays"], ncell, num_hori, group=group)
+    if return_stats:
+        st = dict(st)
+        st["num_rays_total"] = rays
+        st["cell_range"] = (b, e)
+        return h, s, st
+    return h, s

@@ -86,6 +86,14 @@ typedef struct hz_options {
        smallest divisor of num_hori that gives the call at least four search
        items per resident GPU thread (1 for domains that fill the GPU). */
     int32_t mlp_azimuth_groups;
+    /* Given warm start (hz_horizon_svf_device, one domain, in place of the
+       MLP): device int16 [L][num_cell] lattice indices m of the starting
+       elevation m * 0.5 deg (clamped to [-170, 180]), e.g. the horizons of
+       an earlier run on the same grid in quarter degrees (raw_index) halved.
+       Used like the MLP's proposals: at the first azimuth of each search
+       item (mlp_azimuth_groups) or at every azimuth (mlp_every_azimuth).
+       NULL = not used. */
+    const int16_t* start_index;
 } hz_options;
 
 enum {

@@ -21,7 +21,9 @@ _U8 = C.POINTER(C.c_uint8)
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("nthreads", C.c_int),
                 ("cells", _I), ("n_cells", C.c_int),
-                ("elev_floor_deg", C.c_double), ("brute_force", C.c_int)]
+                ("elev_floor_deg", C.c_double), ("brute_force", C.c_int),
+                ("start_m", C.POINTER(C.c_int16)), ("groups", C.c_int),
+                ("start_all", C.c_int)]
 
 
 class Result(C.Structure):
@@ -99,10 +101,14 @@ def _p(a, t):
 
 def horizon_svf(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_type,
                 dist_search, ray_org_elev, refine_factor, svf_type, *, precision=0,
-                nthreads=0, cells=None, elev_floor_deg=-85.0, brute_force=False):
+                nthreads=0, cells=None, elev_floor_deg=-85.0, brute_force=False,
+                start_index=None, groups=1, start_all=False):
     """Oracle horizon [nhori, ncell] (deg), skyview [ncell], stats dict.
 
     With ``cells`` only those columns/entries are computed (others are NaN).
+    ``start_index`` (int16 [L, ncell], L = num_hori * refine_factor): warm
+    start lattice indices; each cell's azimuths form ``groups`` runs whose
+    first azimuth starts there (every azimuth with ``start_all``).
     """
     clon, clat, hsurf, vlon, vlat = map(_f64, (clon, clat, hsurf, vlon, vlat))
     cov = _i32(cells_of_vertex)
@@ -115,6 +121,13 @@ def horizon_svf(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_t
         cells = _i32(cells)
         opt.cells = _p(cells, _I)
         opt.n_cells = cells.size
+    if start_index is not None:
+        start_index = np.ascontiguousarray(start_index, dtype=np.int16)
+        if start_index.shape != (num_hori * refine_factor, ncell):
+            raise ValueError("start_index must have shape (num_hori * refine_factor, ncell)")
+        opt.start_m = start_index.ctypes.data_as(C.POINTER(C.c_int16))
+        opt.groups = int(groups)
+        opt.start_all = int(bool(start_all))
     res = Result()
     rc = lib().hzo_horizon_svf(_p(clon, _D), _p(clat, _D), _p(hsurf, _D), _p(vlon, _D),
                                _p(vlat, _D), _p(cov, _I), _p(horizon, _D),

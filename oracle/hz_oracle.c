@@ -252,6 +252,8 @@ typedef struct {
     double azim_sin, azim_cos, elev_sin_2ha, elev_cos_2ha, azim_shift;
     const int32_t* cells;
     int n_work;
+    const int16_t* start_m;
+    int groups, start_all;
     atomic_int next;
     /* per-run totals */
     atomic_llong rays, nodes, tris, overflow;
@@ -296,7 +298,24 @@ static int64_t trace_cell(const trace_job* J, int i, hzo_counts* cnt) {
     v3d dir = rotate3(north, normal, sin(-J->azim_shift), cos(-J->azim_shift));
     double elev = 0.0;
     double sector = 0.0, svf = 0.0;
+    const int span = J->groups > 1 ? L / J->groups : L;
+    const v3d east = cross3(north, normal);
     for (int a = 0; a < L; a++) {
+        if (J->start_m && (J->start_all || a % span == 0)) {
+            /* Warm start: lattice elevation m at azimuth a, the direction in
+             * closed form cos(e) h_a + sin(e) U with the horizontal direction
+             * h_a = cos(theta_a) N + sin(theta_a) E (the GPU library's form). */
+            int m = J->start_m[(size_t)a * J->ncell + i];
+            m = m < -170 ? -170 : (m > 180 ? 180 : m);
+            elev = (double)m * (2.0 * ha);
+            const double th = J->azim_shift + (double)a * ((2.0 * M_PI) / (double)L);
+            const double ct = cos(th), st = sin(th), ce = cos(elev), se = sin(elev);
+            const v3d hz = {ct * north.x + st * east.x, ct * north.y + st * east.y,
+                            ct * north.z + st * east.z};
+            dir.x = ce * hz.x + se * normal.x;
+            dir.y = ce * hz.y + se * normal.y;
+            dir.z = ce * hz.z + se * normal.z;
+        }
         v3d axis = cross3(dir, normal);
         unit3(&axis);
         int hit = cast_ray(J, &o64, o32, dir, cnt);
@@ -438,6 +457,13 @@ int hzo_horizon_svf(const double* clon, const double* clat, const double* hsurf,
                         + (deg2rad(360.0) / (2.0 * (double)L));
     J.cells = opt.cells;
     J.n_work = opt.cells ? opt.n_cells : ncell;
+    J.start_m = opt.start_m;
+    J.groups = opt.groups;
+    J.start_all = opt.start_all;
+    if (J.start_m && J.groups > 1 && (nhori % J.groups) != 0) {
+        free(enu);
+        return -1;
+    }
     atomic_init(&J.next, 0);
     atomic_init(&J.rays, 0);
     atomic_init(&J.nodes, 0);

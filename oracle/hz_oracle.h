@@ -21,6 +21,15 @@ typedef struct {
     int n_cells;            /* length of `cells` */
     double elev_floor_deg;  /* lower bound of the downward walk (reference: -85) */
     int brute_force;        /* 1: test every triangle instead of the BVH */
+    /* Optional warm start (the GPU library's learned / given start): lattice
+       indices start_m[L][ncell] (elevation m * 0.5 deg, clamped to
+       [-170, 180]). Each cell's azimuths form `groups` runs of L / groups;
+       a run's first azimuth starts at its index instead of the chained
+       elevation (the reference's first azimuth starts at 0, cpp:511), or
+       every azimuth does with start_all. NULL = the reference's chain. */
+    const int16_t* start_m;
+    int groups;
+    int start_all;
 } hzo_options;
 
 typedef struct {
