@@ -47,6 +47,7 @@ WORKLOAD = "500 m ICON-like grid, 600x600 km, fBm(H=0.7)+ridged noise 200-4800 m
 ARGS = (24, 1, 40000.0, 0.2, 1, 2)  # num_hori, grid_type, dist_search, ray_org_elev, refine, svf
 BYTES_PER_NODE = 64
 BYTES_PER_TRI = 48
+EXTRAS = ("learned", "learned_small", "precision", "batch", "drop_in", "configs")
 
 
 def log(*a):
@@ -281,13 +282,16 @@ def train_mlp(make_dom, args=ARGS, n_seeds=8, samples_per_seed=1_000_000, steps=
 def auto_groups(ncell: int, nhori: int) -> int:
     """The library's choice for mlp_azimuth_groups = -1 (hz_options): the
     smallest divisor G of nhori with ncell x G >= 4 x the GPU's resident
-    threads (SMs x 1024), else nhori."""
+    threads (SMs x 1024), at most nhori / 2."""
     import torch
     target = 4 * torch.cuda.get_device_properties(0).multi_processor_count * 1024
-    for g in range(1, nhori + 1):
-        if nhori % g == 0 and ncell * g >= target:
-            return g
-    return nhori
+    pick = 1
+    for g in range(1, nhori // 2 + 1):
+        if nhori % g == 0:
+            pick = g
+            if ncell * g >= target:
+                break
+    return pick
 
 
 LEARNED_MODES = {"first_azimuth": dict(),
@@ -645,15 +649,23 @@ def run_gpu(args):
     # batched uneven-domain workload, the numpy drop-in and the other
     # configurations, each compared with the oracle on a cell sample.
     extras = {}
+    want = set(EXTRAS if args.extras == "all" else args.extras.split(","))
     if not args.no_extras and rank == 0:
-        extras["learned"], mlp = learned_report(dom, d_in, hz, sv, stream, ms, args, sample)
-        extras["learned_small_domains"] = learned_small_report(
-            stream, parity_cells=args.parity_cells)
-        extras["precision"] = precision_report(d_in, hz, stream)
-        extras["batched_domains"] = batch_report(args, mlp)
-        extras["drop_in_numpy"] = drop_in_report(dom, min(args.steps, 3))
-        extras["configs"] = configs_report(dom, d_in, stream,
-                                           parity_cells=args.parity_cells)
+        mlp = None
+        if "learned" in want:
+            extras["learned"], mlp = learned_report(dom, d_in, hz, sv, stream, ms, args, sample)
+        if "learned_small" in want:
+            extras["learned_small_domains"] = learned_small_report(
+                stream, parity_cells=args.parity_cells)
+        if "precision" in want:
+            extras["precision"] = precision_report(d_in, hz, stream)
+        if "batch" in want:
+            extras["batched_domains"] = batch_report(args, mlp)
+        if "drop_in" in want:
+            extras["drop_in_numpy"] = drop_in_report(dom, min(args.steps, 3))
+        if "configs" in want:
+            extras["configs"] = configs_report(dom, d_in, stream,
+                                               parity_cells=args.parity_cells)
     del sample
 
     peak, peak_kind = measured_peaks()
@@ -794,7 +806,9 @@ def main():
                     help="domain width (600 = the benchmark workload; smaller for profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the precision report and the batched-domain run")
+                    help="skip every untimed extra report")
+    ap.add_argument("--extras", default="all",
+                    help="comma-separated extra reports to run: " + ",".join(EXTRAS))
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="target seconds of CPU ray work per CPU measurement")
     ap.add_argument("--parity-cells", type=int, default=20000,

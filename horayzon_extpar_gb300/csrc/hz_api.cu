@@ -964,9 +964,10 @@ int unstage_outputs(Engine& E, const hz_domain& h, const Buffers& b, int begin, 
 // hz_options.mlp_azimuth_groups: 1 without a learned start or for 0 / 1; an
 // explicit G must divide every domain's num_hori; -1 picks, per domain, the
 // smallest divisor G of num_hori that gives the call at least
-// kItemsPerLane x the GPU's resident lanes of search items (num_hori when
-// none does), so that small domains spread each cell's azimuths over G lanes
-// while domains that fill the GPU keep the reference's chain.
+// kItemsPerLane x the GPU's resident lanes of search items (the largest
+// divisor up to num_hori / 2 when none does), so that small domains spread
+// each cell's azimuths over G lanes while domains that fill the GPU keep the
+// reference's chain.
 constexpr int kItemsPerLane = 4;
 
 int azimuth_groups(const hz_domain* doms, int n, const hz_options& opt, int* groups) {
@@ -994,12 +995,16 @@ int azimuth_groups(const hz_domain* doms, int n, const hz_options& opt, int* gro
   for (int d = 0; d < n; d++)
     cells += opt.cell_count > 0 && n == 1 ? opt.cell_count : doms[d].num_cell;
   for (int d = 0; d < n; d++) {
+    // At most num_hori / 2 groups: every item keeps two azimuths of the
+    // chain (an item per azimuth restarts every bracket at its proposal,
+    // which exposes more of the evaluations whose result depends on the
+    // start; see the parity figures of the split modes).
     const int nh = doms[d].num_hori;
-    int pick = nh;
-    for (int g = 1; g <= nh; g++)
-      if (nh % g == 0 && cells * g >= target) {
+    int pick = 1;
+    for (int g = 1; g <= nh / 2; g++)
+      if (nh % g == 0) {
         pick = g;
-        break;
+        if (cells * g >= target) break;
       }
     groups[d] = pick;
   }

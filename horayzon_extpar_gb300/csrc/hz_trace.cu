@@ -483,8 +483,8 @@ __device__ __forceinline__ bool visit_node(const Node* __restrict__ nodes, const
 // Visits BVH4 node `ref`: continues with the nearest hit child and pushes the
 // other hit children, farthest first; pops when no child is hit. Returns false
 // on stack overflow. kTop > 0: references with kTopFlag name the copies of
-// the tree's top nodes in the block's shared memory (s_top), read through
-// generic loads; the others are read from the global tree.
+// the tree's top nodes in the block's shared memory (s_top); the others are
+// read from the global tree.
 template <int kTop = 0>
 __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, const Ray& r,
                                             int& ref, int* stack, int& sp, StackTop& top,
@@ -493,8 +493,8 @@ __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, co
   // of an axis is lo + n (n = 1 for a negative inverse direction).
   float4 nx, fx, ny, fy, nz, fz;
   int4 ch;
-  if (kTop > 0) {
-    const Node4* nd = (ref & kTopFlag) ? s_top + (ref ^ kTopFlag) : nodes4 + ref;
+  if (kTop > 0 && (ref & kTopFlag)) {
+    const Node4* nd = s_top + (ref ^ kTopFlag);
     const float4* pl = reinterpret_cast<const float4*>(nd);
     nx = pl[r.nx]; fx = pl[1 - r.nx];
     ny = pl[2 + r.ny]; fy = pl[3 - r.ny];

@@ -84,7 +84,8 @@ typedef struct hz_options {
        azimuth, so that one cell's azimuths run on G lanes at once (small
        domains fill the GPU). -1: the library picks G per domain, the
        smallest divisor of num_hori that gives the call at least four search
-       items per resident GPU thread (1 for domains that fill the GPU). */
+       items per resident GPU thread (1 for domains that fill the GPU), at
+       most num_hori / 2 (two azimuths per item). */
     int32_t mlp_azimuth_groups;
     /* Given warm start (hz_horizon_svf_device, one domain, in place of the
        MLP): device int16 [L][num_cell] lattice indices m of the starting
