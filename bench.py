@@ -47,6 +47,7 @@ WORKLOAD = "500 m ICON-like grid, 600x600 km, fBm(H=0.7)+ridged noise 200-4800 m
 ARGS = (24, 1, 40000.0, 0.2, 1, 2)  # num_hori, grid_type, dist_search, ray_org_elev, refine, svf
 BYTES_PER_NODE = 64
 BYTES_PER_TRI = 48
+BUILD_BYTES_PER_TRI = 2 * 12 + 36 + 64
 EXTRAS = ("learned", "learned_small", "precision", "batch", "drop_in", "configs")
 
 
@@ -294,9 +295,17 @@ def auto_groups(ncell: int, nhori: int) -> int:
     return pick
 
 
+# The reference walks down to -85 deg (mo_lradtopo_horayzon.cpp:578) where
+# the first ray of a bracket misses; every horizon below -0.25 deg is clipped
+# to 0 (cpp:737-741), so a floor of -0.25 deg gives each azimuth the same
+# output and changes only the elevation carried into the next azimuth
+# (option elev_floor_deg; reported beside the reference's walk).
+FAST_FLOOR_DEG = -0.25
+
 LEARNED_MODES = {"first_azimuth": dict(),
                  "every_azimuth": dict(mlp_every_azimuth=True),
-                 "azimuth_groups_auto": dict(mlp_azimuth_groups=-1)}
+                 "azimuth_groups_auto": dict(mlp_azimuth_groups=-1),
+                 "first_azimuth_fast_floor": dict(elev_floor_deg=FAST_FLOOR_DEG)}
 
 
 def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args, sample=None):
@@ -312,16 +321,19 @@ def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args, sample=None)
     info["seeds"] = "8 other seeds, 120 x 120 km boxes of the same recipe"
     out = {"training": info}
     evals = dom.ncell * ARGS[0]
-    for mode, kw in LEARNED_MODES.items():
+    modes = dict(LEARNED_MODES)
+    modes["plain_fast_floor"] = dict(elev_floor_deg=FAST_FLOOR_DEG)
+    for mode, kw in modes.items():
+        if not mode.startswith("plain"):
+            kw = dict(kw, mlp_params=params)
         for _ in range(max(1, args.warmup)):
-            horizon_svf_comp_device(*d_in, *ARGS, stream=stream, mlp_params=params, **kw)
+            horizon_svf_comp_device(*d_in, *ARGS, stream=stream, **kw)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(args.steps)]
         rays = 0
         for k in range(args.steps):
             ev[k][0].record(stream)
-            h, s, st = horizon_svf_comp_device(*d_in, *ARGS, stream=stream, mlp_params=params,
-                                               **kw)
+            h, s, st = horizon_svf_comp_device(*d_in, *ARGS, stream=stream, **kw)
             ev[k][1].record(stream)
             rays = st["num_rays"]
         torch.cuda.synchronize()
@@ -365,11 +377,14 @@ def learned_small_report(stream, reps=5, parity_cells=20000):
         t = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in d.inputs()]
         evals = d.ncell * ARGS[0]
         res = {"workload": desc, "ncell": d.ncell, "training": info}
+        ff = dict(elev_floor_deg=FAST_FLOOR_DEG)
         modes = {"plain": None, "first_azimuth": {}, "azimuth_groups_auto":
-                 {"mlp_azimuth_groups": -1}}
+                 {"mlp_azimuth_groups": -1}, "plain_fast_floor": ff,
+                 "azimuth_groups_auto_fast_floor": dict(ff, mlp_azimuth_groups=-1)}
         sample = oracle_sample(d, ARGS, parity_cells) if parity_cells > 0 else None
         for mode, kw in modes.items():
-            extra = {} if kw is None else dict(mlp_params=params, **kw)
+            extra = {} if kw is None else (dict(kw) if mode.startswith("plain") else
+                                           dict(mlp_params=params, **kw))
             horizon_svf_comp_device(*t, *ARGS, stream=stream, **extra)  # warm-up
             best = None
             for _ in range(reps):
@@ -381,14 +396,19 @@ def learned_small_report(stream, reps=5, parity_cells=20000):
                          "evals_per_s_search": evals / (best["ms_trace"] * 1e-3),
                          "evals_per_s_call": evals / (call_ms * 1e-3),
                          "rays_per_eval": best["num_rays"] / evals}
-            if mode == "azimuth_groups_auto":
+            if mode.startswith("azimuth_groups_auto"):
                 res[mode]["groups"] = auto_groups(d.ncell, ARGS[0])
             if sample is not None:
                 res[mode]["parity"] = parity_block(h.cpu().numpy(), s.cpu().numpy(), sample)
-        for mode in ("first_azimuth", "azimuth_groups_auto"):
-            res[mode]["speedup_vs_plain_search"] = (res["plain"]["search_ms"] /
-                                                    res[mode]["search_ms"])
-            res[mode]["speedup_vs_plain_call"] = res["plain"]["call_ms"] / res[mode]["call_ms"]
+        for mode, base in (("first_azimuth", "plain"), ("azimuth_groups_auto", "plain"),
+                           ("plain_fast_floor", "plain"),
+                           ("azimuth_groups_auto_fast_floor", "plain"),
+                           ("azimuth_groups_auto_fast_floor", "plain_fast_floor")):
+            tag = "" if base == "plain" else "_fast_floor"
+            res[mode]["speedup_vs_plain%s_search" % tag] = (res[base]["search_ms"] /
+                                                            res[mode]["search_ms"])
+            res[mode]["speedup_vs_plain%s_call" % tag] = (res[base]["call_ms"] /
+                                                          res[mode]["call_ms"])
         out[key] = res
         del t
     return out
@@ -671,6 +691,11 @@ def run_gpu(args):
     peak, peak_kind = measured_peaks()
     alg_bytes = BYTES_PER_NODE * st_count["node_visits"] + BYTES_PER_TRI * st_count["tri_tests"]
     achieved = alg_bytes / (trace_ms * 1e-3) / 1e9
+    # LBVH build phase: 2 sort passes x 12 B + 36 B triangle + 64 B node per
+    # triangle, over the phase's CUDA-event time.
+    bvh_ms = float(np.mean([s["ms_bvh"] for s in stats]))
+    build_bytes = BUILD_BYTES_PER_TRI * st_count["n_tri"]
+    build_achieved = build_bytes / (bvh_ms * 1e-3) / 1e9
     traffic = traffic_from_profile()
 
     if rank != 0:
@@ -723,7 +748,12 @@ def run_gpu(args):
                      "node_visits_per_ray": st_count["node_visits"] / rays,
                      "tri_tests_per_ray": st_count["tri_tests"] / rays,
                      "bvh4_node_visits_per_ray": st_wide["node_visits"] / rays,
-                     "bvh4_tri_tests_per_ray": st_wide["tri_tests"] / rays},
+                     "bvh4_tri_tests_per_ray": st_wide["tri_tests"] / rays,
+                     "build_bytes_per_triangle": BUILD_BYTES_PER_TRI,
+                     "build_bytes_per_launch": build_bytes, "build_ms": bvh_ms,
+                     "build_achieved": build_achieved, "build_frac": build_achieved / peak,
+                     "build_bound": "latency (bottom-up refit chains) and issue (Karras "
+                                    "splits)"},
         "parity": parity,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),

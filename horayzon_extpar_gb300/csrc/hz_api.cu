@@ -124,6 +124,7 @@ struct Buffers {
   unsigned* rz_bits;
   float* rz;
   long long raster_budget;
+  RasterDesc* rdesc;   // device descriptor of the raster
   int16_t* start_m;
   double* svf_part;    // split learned start with refine_factor > 1: [groups][ncell]
   double* cell_enu;
@@ -132,8 +133,6 @@ struct Buffers {
   // BVH
   Node* nodes;
   Node4* nodes4;     // wide traversal only
-  Node4* top4;       // wide traversal: copies of the top nodes (shared-memory staging)
-  int* n_top;
   Tri* tris;
   BvhScratch bvh;
   // search
@@ -185,11 +184,7 @@ Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhor
   b.cell_origin = c.take<float>(6 * ncell);
   const long long nt = max_tri > 0 ? max_tri : 1;
   b.nodes = c.take<Node>(nt > 1 ? nt - 1 : 1);
-  if (wide) {
-    b.nodes4 = c.take<Node4>(nt > 1 ? nt - 1 : 1);
-    b.top4 = c.take<Node4>(kTopNodesLarge);
-    b.n_top = c.take<int>(4);
-  }
+  if (wide) b.nodes4 = c.take<Node4>(nt > 1 ? nt - 1 : 1);
   b.tris = c.take<Tri>(nt);
   if (precise) {
     b.vert_lo = c.take<float>(3 * max_mv);
@@ -199,6 +194,7 @@ Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhor
     b.raster_budget = max_mv + max_mv / 10 + 4096;
     b.rz_bits = c.take<unsigned>(b.raster_budget);
     b.rz = c.take<float>(b.raster_budget);
+    b.rdesc = c.take<RasterDesc>(1);
     b.start_m = c.take<int16_t>(L * ncell);
   }
   if (svf_part_len > 0) b.svf_part = c.take<double>(svf_part_len);
@@ -210,6 +206,7 @@ Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhor
   b.bvh.parent = c.take<int>(nt);
   b.bvh.nsize = c.take<int>(nt);
   b.bvh.counter = c.take<int>(nt);
+  b.bvh.cost = c.take<float>(nt);
   b.bvh.bounds = c.take<unsigned>(16);
   b.bvh.sort_scratch = c.take<char>(radix_scratch_u32(nt));
   b.order_scratch = c.take<char>(cell_order_scratch_bytes(ncell));
@@ -464,20 +461,8 @@ struct RunOut {
 // Runs the pipeline for n domains whose arrays are device pointers in pr[].
 // With stop != kFull it ends after the mesh (or ENU) stage and leaves the
 // results in b[].
-// Top nodes of the 4-wide tree staged in shared memory by the search
-// (single-domain calls): HZ_TOP_NODES = 0 (none), 21 or 85.
-int top_nodes_setting() {
-  static const int v = [] {
-    const char* e = getenv("HZ_TOP_NODES");
-    const int x = e ? atoi(e) : 0;
-    return x >= kTopNodesLarge ? kTopNodesLarge : (x >= kTopNodesSmall ? kTopNodesSmall : 0);
-  }();
-  return v;
-}
-
 int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const BatchBuffers& bb,
               cudaStream_t s, const hz_options& opt, hz_stats* st, Stop stop, RunOut* out) {
-  const int top_nodes = opt.kernel == HZ_KERNEL_PERSISTENT ? top_nodes_setting() : 0;
   g_launches = 0;
   g_log.clear();
   out->n_tri.assign(n, 0);
@@ -575,14 +560,16 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     out->origin_lon[d] = rad2deg(atan2(so[1], so[0]));
   }
 
-  // From here to the readback the host waits for nothing (except for the
-  // learned start's raster sizing): the work is captured into a CUDA graph,
-  // kept on the engine and updated in place for the next call of the same
-  // shape, and launched as one unit.
-  const bool learned_run = stop == Stop::kFull && b[0].rz != nullptr;
+  // From here to the readback the host waits for nothing: the work is
+  // captured into a CUDA graph, kept on the engine and updated in place for
+  // the next call of the same shape, and launched as one unit. The learned
+  // start's parameters are copied before (a pageable host source).
+  if (stop == Stop::kFull && b[0].rz != nullptr && opt.mlp_params)
+    HZ_CUDA(cudaMemcpyAsync(bb.mlp, opt.mlp_params, sizeof(float) * kMlpParams,
+                            cudaMemcpyHostToDevice, s));
   cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
   HZ_CUDA(cudaStreamIsCapturing(s, &cap_status));
-  Capture cap(E.stream, s, stop == Stop::kFull && !learned_run && !opt.direct_launch &&
+  Capture cap(E.stream, s, stop == Stop::kFull && !opt.direct_launch &&
                      opt.kernel != HZ_KERNEL_PER_CELL &&
                      cap_status == cudaStreamCaptureStatusNone);
   HZ_CUDA(cap.begin());
@@ -606,11 +593,8 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     HZ_CUDA(fk.begin());
     for (int d = 0; d < n; d++) {
       HZ_CUDA(bvh_build(b[d].vert32, b[d].vot, out->n_tri[d], b[d].nodes, b[d].tris, b[d].bvh,
-                        fk.on(d), b[d].vert_lo, b[d].tri_lo, b[d].nodes4, opt.leaf_size));
-      if (n == 1 && b[d].nodes4 && top_nodes > 0)
-        HZ_CUDA(bvh_stage_top4(b[d].nodes4, out->n_tri[d],
-                               top_nodes >= kTopNodesLarge ? 4 : 3, b[d].top4, b[d].n_top,
-                               fk.on(d)));
+                        fk.on(d), b[d].vert_lo, b[d].tri_lo, b[d].nodes4, opt.leaf_size,
+                        opt.bvh_treelets != 0));
     }
     HZ_CUDA(fk.end());
   }
@@ -662,49 +646,10 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
   } else {
     DomainDesc* desc = reinterpret_cast<DomainDesc*>(pin + 64 + 5 * (size_t)n + 8);
     // Learned warm start: height rasters over each domain's triangle-centre
-    // bounds (read back from the BVH build), then features + MLP.
+    // bounds (from the BVH build, on the device), then features + MLP.
     const bool learned = b[0].rz != nullptr;
-    std::vector<RasterDesc> rdesc(n);
-    if (learned) {
-      if (opt.mlp_params)
-        HZ_CUDA(cudaMemcpyAsync(bb.mlp, opt.mlp_params, sizeof(float) * kMlpParams,
-                                cudaMemcpyHostToDevice, s));
-      unsigned* pb = reinterpret_cast<unsigned*>(pin + 64 + 2 * n);  // 4 per domain
-      for (int d = 0; d < n; d++)
-        if (out->n_tri[d] > 0)
-          HZ_CUDA(cudaMemcpyAsync(pb + 4 * d, b[d].bvh.bounds, 4 * sizeof(unsigned),
-                                  cudaMemcpyDeviceToHost, s));
-      HZ_CUDA(cudaStreamSynchronize(s));
-      for (int d = 0; d < n; d++) {
-        RasterDesc R;
-        std::memset(&R, 0, sizeof(R));
-        R.nx = R.ny = 1;
-        R.dx = R.inv_dx = 1.f;
-        if (out->n_tri[d] > 0) {
-          const float x0 = ord2f_host(pb[4 * d]), y0 = ord2f_host(pb[4 * d + 1]);
-          const float x1 = ord2f_host(pb[4 * d + 2]), y1 = ord2f_host(pb[4 * d + 3]);
-          const double ex = std::max(1.0, (double)x1 - x0), ey = std::max(1.0, (double)y1 - y0);
-          double dx = sqrt(ex * ey / (0.9 * (double)b[d].raster_budget));
-          for (;;) {
-            const long long nx = (long long)ceil(ex / dx) + 8, ny = (long long)ceil(ey / dx) + 8;
-            if (nx * ny <= b[d].raster_budget) {
-              R.nx = (int)nx;
-              R.ny = (int)ny;
-              break;
-            }
-            dx *= 1.05;
-          }
-          R.dx = (float)dx;
-          R.inv_dx = (float)(1.0 / dx);
-          R.x0 = (float)(x0 - 4.0 * dx);
-          R.y0 = (float)(y0 - 4.0 * dx);
-        }
-        R.z = b[d].rz;
-        rdesc[d] = R;
-      }
-    }
     long long total = 0, total_items = 0;
-    Fork fk(E, s, learned ? 1 : n);  // the learned start's kernels stay on s
+    Fork fk(E, s, n);
     HZ_CUDA(fk.begin());
     for (int d = 0; d < n; d++) {
       const Problem& P = pr[d];
@@ -712,8 +657,8 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       HZ_CUDA(trace_tables(b[d].azim_cs, b[d].elev_cs, b[d].svf_lattice, L, shift[d],
                            hori_acc, P.svf_type, fk.on(d)));
       if (learned) {
-        HZ_CUDA(raster_build(b[d].vert32, b[d].vot, out->n_tri[d], rdesc[d], b[d].rz_bits,
-                             b[d].rz, s));
+        HZ_CUDA(raster_build(b[d].vert32, b[d].vot, out->n_tri[d], b[d].bvh.bounds,
+                             b[d].raster_budget, b[d].rdesc, b[d].rz_bits, b[d].rz, fk.on(d)));
         LearnParams q;
         std::memset(&q, 0, sizeof(q));
         q.cell_enu = b[d].cell_enu;
@@ -737,10 +682,10 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
         }
         q.dist_search = (float)P.dist_search;
         q.azim_cs = b[d].azim_cs;
-        q.raster = rdesc[d];
+        q.raster = b[d].rdesc;
         q.features = n == 1 ? opt.features : nullptr;
         q.start_m = b[d].start_m;
-        HZ_CUDA(learn_features(q, opt.mlp_params ? bb.mlp : nullptr, s));
+        HZ_CUDA(learn_features(q, opt.mlp_params ? bb.mlp : nullptr, fk.on(d)));
       }
       HZ_CUDA(cell_order(b[d].cell_enu, P.cell_begin, P.cell_count, (int)(total - P.cell_begin),
                          bb.order + total, b[d].order_scratch, b[d].cell_bounds, bb.work,
@@ -767,8 +712,6 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.groups = P.groups;
       D.item_begin = total_items;
       D.svf_part = b[d].svf_part;
-      D.top4 = n == 1 && top_nodes > 0 ? b[d].top4 : nullptr;
-      D.n_top = b[d].n_top;
       D.raw_j = n == 1 ? opt.raw_index : nullptr;
       D.centre = frames[d].centre;
       D.pole = frames[d].pole;
@@ -803,7 +746,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     k_stamp<<<1, 1, 0, s>>>(bb.t0);
     note_launches(1);
     HZ_CUDA(cudaGetLastError());
-    const TraceKnobs knobs{adv, leaf, opt.queue_chunk, variant, n == 1 ? top_nodes : 0};
+    const TraceKnobs knobs{adv, leaf, opt.queue_chunk, variant};
     HZ_CUDA(trace_flat(bb.doms, n, bb.order, (int)total, (int)total_items, bb.work,
                        bb.counters, bb.err, knobs, opt.count_work != 0,
                        b[0].tri_lo != nullptr, s));
@@ -1442,6 +1385,7 @@ int hz_occluded32(const float* vert, int n_vert, const int32_t* vertex_of_triang
     sc.parent = c.take<int>(nt);
     sc.nsize = c.take<int>(nt);
     sc.counter = c.take<int>(nt);
+    sc.cost = c.take<float>(nt);
     sc.bounds = c.take<unsigned>(16);
     sc.sort_scratch = c.take<char>(radix_scratch_u32(nt));
   };

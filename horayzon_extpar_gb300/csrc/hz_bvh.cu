@@ -11,7 +11,10 @@
 //      leaves;
 //   5. k_gather: 48-byte triangle records in leaf order;
 //   6. k_refit: bottom-up boxes with one atomic arrival counter per node;
-//   7. optionally k_collapse4: the 4-wide tree used by the wide traversal.
+//   7. optionally k_treelet: treelet restructuring (Karras & Aila, "Fast
+//      parallel construction of high-quality bounding volume hierarchies",
+//      HPG 2013) with treelets of 5 leaves, bottom-up like the refit;
+//   8. optionally k_collapse4: the 4-wide tree used by the wide traversal.
 // Child boxes carry a margin of 2^-20 x the largest coordinate so that box
 // culling never hides a triangle the watertight test would report. The tree
 // has the same topology as the CPU oracle's (same keys, same splits).
@@ -219,6 +222,180 @@ __global__ void k_refit(Node* __restrict__ nodes, const Tri* __restrict__ tris, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Treelet restructuring. Each live node R, once both of its subtrees are
+// done, forms a treelet of up to kTreelet leaves: its two children, then
+// repeatedly the treelet leaf with the largest cost area that is an internal
+// node replaced by its two children. Dynamic programming over the subsets of
+// the leaves finds the binary topology of least cost
+//   C(node) = kCi * A(node) + C(left) + C(right),  C(leaf) = kCt * count * A(leaf)
+// (A: the cost area below), the treelet's internal nodes are rewired to it
+// (same node indices, the leaves untouched) and C(R) is kept for R's
+// ancestors. Box tests stay conservative (every box is the union of the
+// original padded leaf boxes), so the searches' results do not change.
+// Cost area: (dx + dy) dz + 0.1 dx dy -- the projected area for the near-
+// horizontal rays of the search plus a share of the footprint (ray origins
+// lie on the terrain inside it).
+// ---------------------------------------------------------------------------
+constexpr int kTreelet = 5;
+constexpr float kCi = 1.2f, kCt = 1.0f;
+
+__device__ __forceinline__ float cost_area(const Box& b) {
+  const float dx = b.hx - b.lx, dy = b.hy - b.ly, dz = b.hz - b.lz;
+  if (!(dx >= 0.f)) return 0.f;  // empty
+  return (dx + dy) * dz + 0.1f * dx * dy;
+}
+__device__ __forceinline__ Box box_union(const Box& a, const Box& b) {
+  return Box{fminf(a.lx, b.lx), fminf(a.ly, b.ly), fminf(a.lz, b.lz),
+             fmaxf(a.hx, b.hx), fmaxf(a.hy, b.hy), fmaxf(a.hz, b.hz)};
+}
+// Child `side` of node: reference and box (coherent loads: other threads of
+// the same launch wrote them).
+__device__ __forceinline__ void load_child(const Node* node, int side, int& ref, Box& b) {
+  const float* base = reinterpret_cast<const float*>(node);
+  const float4 xy = __ldcg(reinterpret_cast<const float4*>(base + 4 * side));
+  const float2 z = __ldcg(reinterpret_cast<const float2*>(base + 8 + 2 * side));
+  const float2 d = __ldcg(reinterpret_cast<const float2*>(base + 12));
+  ref = __float_as_int(side ? d.y : d.x);
+  b = Box{xy.x, xy.z, z.x, xy.y, xy.w, z.y};
+}
+__device__ __forceinline__ void store_node(Node* node, int r0, const Box& b0, int r1,
+                                           const Box& b1) {
+  __stcg(&node->a, make_float4(b0.lx, b0.hx, b0.ly, b0.hy));
+  __stcg(&node->b, make_float4(b1.lx, b1.hx, b1.ly, b1.hy));
+  __stcg(&node->c, make_float4(b0.lz, b0.hz, b1.lz, b1.hz));
+  __stcg(&node->d, make_float4(__int_as_float(r0), __int_as_float(r1), 0.f, 0.f));
+}
+
+// Restructures the treelet rooted at live node R and stores C(R).
+__device__ void treelet_at(Node* nodes, int R, int* parent, int* nsize, float* cost,
+                           int leaf_max) {
+  int lref[kTreelet];
+  Box lbox[kTreelet];
+  float lcost[kTreelet];
+  int pool[kTreelet - 1];
+  int nl = 0, np = 0;
+  pool[np++] = R;
+  for (int side = 0; side < 2; side++) {
+    int r;
+    Box b;
+    load_child(nodes + R, side, r, b);
+    if (r == kEmptyRef) continue;
+    lref[nl] = r;
+    lbox[nl] = b;
+    nl++;
+  }
+  while (nl < kTreelet) {
+    int best = -1;
+    float ba = -1.f;
+    for (int k = 0; k < nl; k++)
+      if (lref[k] >= 0) {
+        const float a = cost_area(lbox[k]);
+        if (a > ba) {
+          ba = a;
+          best = k;
+        }
+      }
+    if (best < 0) break;
+    const int X = lref[best];
+    pool[np++] = X;
+    load_child(nodes + X, 0, lref[best], lbox[best]);
+    load_child(nodes + X, 1, lref[nl], lbox[nl]);
+    nl++;
+  }
+  for (int k = 0; k < nl; k++)
+    lcost[k] = lref[k] >= 0 ? __ldcg(cost + lref[k])
+                            : kCt * (float)leaf_count(lref[k]) * cost_area(lbox[k]);
+  if (nl < 3) {
+    const Box u = nl == 2 ? box_union(lbox[0], lbox[1]) : lbox[0];
+    __stcg(cost + R, kCi * cost_area(u) + lcost[0] + (nl == 2 ? lcost[1] : 0.f));
+    return;
+  }
+  constexpr int kSets = 1 << kTreelet;
+  float copt[kSets];
+  Box ubox[kSets];
+  unsigned char bestp[kSets];
+  const int full = (1 << nl) - 1;
+  for (int st = 1; st <= full; st++) {
+    const int low = __ffs(st) - 1;
+    if ((st & (st - 1)) == 0) {
+      copt[st] = lcost[low];
+      ubox[st] = lbox[low];
+      continue;
+    }
+    ubox[st] = box_union(ubox[st & (st - 1)], lbox[low]);
+    // Partitions (p, st ^ p) with p holding the lowest member of st.
+    const int lowbit = st & -st;
+    float c = INFINITY;
+    int bp = 0;
+    for (int p = (st - 1) & st; p; p = (p - 1) & st) {
+      if (!(p & lowbit)) continue;
+      const float cp = copt[p] + copt[st ^ p];
+      if (cp < c) {
+        c = cp;
+        bp = p;
+      }
+    }
+    copt[st] = kCi * cost_area(ubox[st]) + c;
+    bestp[st] = (unsigned char)bp;
+  }
+  // Rewire: node pool[k] takes the k-th internal subset in depth-first order.
+  int qs[kTreelet], qn[kTreelet], qh = 0, used = 1;
+  qs[qh] = full;
+  qn[qh] = R;
+  qh++;
+  while (qh > 0) {
+    qh--;
+    const int st = qs[qh], node = qn[qh];
+    const int part[2] = {bestp[st], st ^ bestp[st]};
+    int ref[2];
+    for (int side = 0; side < 2; side++) {
+      const int q = part[side];
+      if ((q & (q - 1)) == 0) {
+        ref[side] = lref[__ffs(q) - 1];
+        if (ref[side] >= 0) parent[ref[side]] = (node << 1) | side;
+      } else {
+        const int nd = pool[used++];
+        ref[side] = nd;
+        parent[nd] = (node << 1) | side;
+        nsize[nd] = max(nsize[nd], leaf_max + 1);  // live (k_collapse4)
+        __stcg(cost + nd, copt[q]);
+        qs[qh] = q;
+        qn[qh] = nd;
+        qh++;
+      }
+    }
+    store_node(nodes + node, ref[0], ubox[part[0]], ref[1], ubox[part[1]]);
+  }
+  __stcg(cost + R, copt[full]);
+}
+
+// Bottom-up over the live nodes (arrival counters as in k_refit, which left
+// them at 2: cleared before this launch).
+__global__ void k_treelet(Node* __restrict__ nodes, int n, int* __restrict__ parent,
+                          int* __restrict__ nsize, int* __restrict__ counter,
+                          float* __restrict__ cost, int leaf_max) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1 || nsize[i] <= leaf_max) return;
+  const float4 d = nodes[i].d;
+  const int arrivals = (__float_as_int(d.x) < 0) + (__float_as_int(d.y) < 0);
+  if (arrivals == 0) return;
+  __threadfence();
+  int old = atomicAdd(&counter[i], arrivals);
+  if (old + arrivals != 2) return;
+  int node = i;
+  for (;;) {
+    __threadfence();
+    treelet_at(nodes, node, parent, nsize, cost, leaf_max);
+    if (node == 0) return;
+    const int p = __ldcg(parent + node) >> 1;
+    __threadfence();
+    old = atomicAdd(&counter[p], 1);
+    if (old + 1 != 2) return;
+    node = p;
+  }
+}
+
 // n_tri <= leaf_max: one node, child 0 = leaf of all triangles, child 1 empty.
 __global__ void k_small_root(Node* nodes, const Tri* __restrict__ tris, int n,
                              const unsigned* __restrict__ bounds) {
@@ -279,53 +456,7 @@ __global__ void k_collapse4(const Node* __restrict__ nodes, int n_nodes,
   out[i] = q;
 }
 
-// Level-synchronous walk of the top levels of the 4-wide tree by one block:
-// copies each visited node into top4 and renames its children that are
-// copied too (next level) to kTopFlag | slot.
-__global__ void k_stage_top4(const Node4* __restrict__ nodes4, int levels,
-                             Node4* __restrict__ top4, int* __restrict__ n_top) {
-  __shared__ int queue[kTopNodesLarge];
-  __shared__ int count;
-  if (threadIdx.x == 0) {
-    queue[0] = 0;
-    count = 1;
-  }
-  __syncthreads();
-  int begin = 0, end = 1;
-  for (int level = 0; level < levels; level++) {
-    for (int i = begin + threadIdx.x; i < end; i += blockDim.x) {
-      Node4 nd = nodes4[queue[i]];
-      int ch[4] = {nd.child.x, nd.child.y, nd.child.z, nd.child.w};
-      if (level + 1 < levels) {
-        for (int j = 0; j < 4; j++) {
-          if (ch[j] < 0) continue;  // leaf or empty
-          const int slot = atomicAdd(&count, 1);  // < kTopNodesLarge for levels <= 4
-          queue[slot] = ch[j];
-          ch[j] = kTopFlag | slot;
-        }
-      }
-      nd.child = make_int4(ch[0], ch[1], ch[2], ch[3]);
-      top4[i] = nd;
-    }
-    __syncthreads();
-    begin = end;
-    end = count;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *n_top = begin;
-}
-
 }  // namespace
-
-cudaError_t bvh_stage_top4(const Node4* nodes4, int n_tri, int levels, Node4* top4, int* n_top,
-                           cudaStream_t s) {
-  if (levels < 1) levels = 1;
-  if (levels > 4) levels = 4;
-  if (n_tri <= 0) return cudaMemsetAsync(n_top, 0, sizeof(int), s);
-  k_stage_top4<<<1, 128, 0, s>>>(nodes4, levels, top4, n_top);
-  note_launches(1);
-  return cudaGetLastError();
-}
 
 size_t bvh_scratch_bytes(long long n) {
   if (n < 1) n = 1;
@@ -333,6 +464,7 @@ size_t bvh_scratch_bytes(long long n) {
   b += 4 * sizeof(uint32_t) * (size_t)n;  // keys, vals, keys_alt, vals_alt
   b += sizeof(float2) * (size_t)n;
   b += 3 * sizeof(int) * (size_t)n;       // parent, nsize, counter
+  b += sizeof(float) * (size_t)n;         // cost (treelets)
   b += 64;                                // bounds
   b += radix_scratch_u32(n);
   return b + 8 * 256;                     // alignment slack
@@ -340,7 +472,7 @@ size_t bvh_scratch_bytes(long long n) {
 
 cudaError_t bvh_build(const float* vert32, const int* vot, int n, Node* nodes, Tri* tris,
                       const BvhScratch& sc, cudaStream_t s, const float* vert_lo,
-                      float4* tri_lo, Node4* nodes4, int leaf_max) {
+                      float4* tri_lo, Node4* nodes4, int leaf_max, bool treelets) {
   if (leaf_max < 1 || leaf_max > 8) leaf_max = kLeafMax;
   if (n <= 0) return cudaSuccess;
   k_init_bounds<<<1, 1, 0, s>>>(sc.bounds);
@@ -366,6 +498,13 @@ cudaError_t bvh_build(const float* vert32, const int* vot, int n, Node* nodes, T
                                                 sc.counter, leaf_max);
   k_refit<<<grid_for(n - 1, 256), 256, 0, s>>>(nodes, tris, n, sc.parent, sc.nsize,
                                                sc.counter, sc.bounds, leaf_max);
+  if (treelets && sc.cost) {
+    cudaError_t e = cudaMemsetAsync(sc.counter, 0, sizeof(int) * (size_t)(n - 1), s);
+    if (e != cudaSuccess) return e;
+    k_treelet<<<grid_for(n - 1, 256), 256, 0, s>>>(nodes, n, sc.parent, sc.nsize, sc.counter,
+                                                   sc.cost, leaf_max);
+    note_launches(1);
+  }
   if (nodes4) {
     k_collapse4<<<grid_for(n - 1, 256), 256, 0, s>>>(nodes, n - 1, sc.nsize, leaf_max,
                                                      nodes4);

@@ -59,14 +59,6 @@ struct __align__(16) Node4 {
 };
 constexpr int kStackDepth4 = 96;  // 3 pushes per BVH4 level
 
-// Copies of the top levels of a 4-wide tree for staging in shared memory: a
-// child reference with kTopFlag set names slot (ref ^ kTopFlag) of the copy
-// (tree node indices stay below 2^27). Two levels below the root hold at most
-// 1 + 4 + 16 nodes, three at most 85.
-constexpr int kTopFlag = 1 << 30;
-constexpr int kTopNodesSmall = 21;
-constexpr int kTopNodesLarge = 85;
-
 // Triangle record, 48 bytes, one float4 per axis: x = (v0.x, v1.x, v2.x,
 // original id), y = (v0.y, v1.y, v2.y, 0), z = (v0.z, v1.z, v2.z, 0). A ray
 // loads the axes in its own (kx, ky, kz) order by address offset.

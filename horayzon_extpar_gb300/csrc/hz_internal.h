@@ -67,6 +67,7 @@ struct BvhScratch {
   int* parent;          // n (node -> parent << 1 | side)
   int* nsize;           // n (range size per internal node)
   int* counter;         // n (refit arrivals)
+  float* cost;          // n (treelet costs; optional)
   unsigned* bounds;     // 5: min cx, min cy, max cx, max cy, max |coord| (ordered)
   void* sort_scratch;   // radix_scratch_u32(n)
 };
@@ -77,16 +78,13 @@ size_t bvh_scratch_bytes(long long n_tri);
 // With vert_lo, also writes tri_lo[3 * n_tri]: the FP32 residuals of v0, v1,
 // v2 per triangle in leaf order (precise mode). With nodes4 (same length as
 // nodes), also the BVH4 collapse of the tree (root 0).
+// treelets: restructure the binary tree by treelets (k_treelet; needs
+// sc.cost) before the collapse.
 cudaError_t bvh_build(const float* vert32, const int* vot, int n_tri, Node* nodes,
                       Tri* tris, const BvhScratch& sc, cudaStream_t s,
                       const float* vert_lo = nullptr, float4* tri_lo = nullptr,
-                      Node4* nodes4 = nullptr, int leaf_max = kLeafMax);
-
-// Copies of the top `levels` levels (1..4) of the 4-wide tree (root 0) into
-// top4[<= kTopNodesLarge], child references between copied nodes rewritten to
-// kTopFlag | slot (slot 0 = the root); the node count goes to *n_top.
-cudaError_t bvh_stage_top4(const Node4* nodes4, int n_tri, int levels, Node4* top4, int* n_top,
-                           cudaStream_t s);
+                      Node4* nodes4 = nullptr, int leaf_max = kLeafMax,
+                      bool treelets = false);
 
 // ---- hz_trace.cu ------------------------------------------------------------
 struct TraceParams {
@@ -174,8 +172,6 @@ struct DomainDesc {
   int root, ncell, ncell_traced, nhori, refine, L, svf_type;
   int n_tri;                  // triangles of the tree (nodes: max(1, n_tri - 1))
   float tfar;
-  const Node4* top4;          // optional: copies of the tree's top nodes (bvh_stage_top4)
-  const int* n_top;           // device: nodes in top4
 };
 
 // Persistent flattened search (same rays and results as trace_exact) over
@@ -203,8 +199,6 @@ struct TraceKnobs {
   int leaf_min;     // 1..32
   int chunk;        // work ids a warp claims per atomic (< 1: kDefaultChunk)
   int variant;      // kTrace*
-  int top_nodes;    // 4-wide tree, single domain: top nodes staged in shared memory
-                    // (0, kTopNodesSmall or kTopNodesLarge; needs DomainDesc::top4)
 };
 // `total` traced cells (frames, epilogue) and `total_items` search items
 // (the sum of groups x traced cells over the domains).
@@ -252,13 +246,17 @@ struct LearnParams {
   int n_pred, a_stride;  // azimuths q * a_stride, q < n_pred, get features / predictions
   float dist_search;
   const double2* azim_cs;
-  RasterDesc raster;
+  const RasterDesc* raster;  // device (raster_build)
   float* features;   // optional [L][ncell][32]
   int16_t* start_m;  // with params: learned start lattice index [L][ncell]
 };
 
-cudaError_t raster_build(const float* vert32, const int* vot, int n_tri, RasterDesc R,
-                         unsigned* zbits, float* z, cudaStream_t s);
+// The height raster of a domain: descriptor (sized from the BVH build's
+// triangle-centre bounds, at most `budget` texels) to *rdesc on the device,
+// then the maximum height of the covering triangles per texel into z.
+cudaError_t raster_build(const float* vert32, const int* vot, int n_tri, const unsigned* bounds,
+                         long long budget, RasterDesc* rdesc, unsigned* zbits, float* z,
+                         cudaStream_t s);
 // Features of every traced (cell, azimuth); with params (FP32, kMlpParams,
 // device) also the MLP's start index.
 cudaError_t learn_features(const LearnParams& q, const float* params, cudaStream_t s);

@@ -240,15 +240,50 @@ __device__ __forceinline__ void store_row_bf16(__nv_bfloat16* row, const float (
 // ---------------------------------------------------------------------------
 // Height raster
 // ---------------------------------------------------------------------------
+// The raster over the triangle-centre bounds of the BVH build (ordered
+// floats: min x, min y, max x, max y) with a margin of 4 texels: square
+// texels, as fine as `budget` texels allow. One thread; the descriptor stays
+// on the device, so the learned start needs no host readback.
+__global__ void k_raster_setup(const unsigned* __restrict__ bounds, int n_tri, long long budget,
+                               float* z, RasterDesc* __restrict__ out) {
+  RasterDesc R;
+  R.nx = R.ny = 1;
+  R.dx = R.inv_dx = 1.f;
+  R.x0 = R.y0 = 0.f;
+  if (n_tri > 0) {
+    const float x0 = ord2f(bounds[0]), y0 = ord2f(bounds[1]);
+    const float x1 = ord2f(bounds[2]), y1 = ord2f(bounds[3]);
+    const double ex = fmax(1.0, (double)x1 - x0), ey = fmax(1.0, (double)y1 - y0);
+    double dx = sqrt(ex * ey / (0.9 * (double)budget));
+    for (int it = 0; it < 200; it++) {
+      const long long nx = (long long)ceil(ex / dx) + 8, ny = (long long)ceil(ey / dx) + 8;
+      if (nx * ny <= budget) {
+        R.nx = (int)nx;
+        R.ny = (int)ny;
+        break;
+      }
+      dx *= 1.05;
+    }
+    R.dx = (float)dx;
+    R.inv_dx = (float)(1.0 / dx);
+    R.x0 = (float)(x0 - 4.0 * dx);
+    R.y0 = (float)(y0 - 4.0 * dx);
+  }
+  R.z = z;
+  *out = R;
+}
+
 __global__ void k_raster_fill(unsigned* __restrict__ z, long long n) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) z[i] = 0u;  // below every ordered float: "no terrain"
 }
 
 __global__ void k_raster_tris(const float* __restrict__ vert, const int* __restrict__ vot,
-                              int n_tri, RasterDesc R, unsigned* __restrict__ z) {
+                              int n_tri, const RasterDesc* __restrict__ Rp,
+                              unsigned* __restrict__ z) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_tri) return;
+  const RasterDesc R = *Rp;
   const int i0 = vot[3LL * t], i1 = vot[3LL * t + 1], i2 = vot[3LL * t + 2];
   const float ax = vert[3LL * i0], ay = vert[3LL * i0 + 1], az = vert[3LL * i0 + 2];
   const float bx = vert[3LL * i1], by = vert[3LL * i1 + 1], bz = vert[3LL * i1 + 2];
@@ -276,9 +311,9 @@ __global__ void k_raster_tris(const float* __restrict__ vert, const int* __restr
 }
 
 __global__ void k_raster_finish(const unsigned* __restrict__ zi, float* __restrict__ zf,
-                                long long n) {
+                                const RasterDesc* __restrict__ Rp) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) zf[i] = zi[i] == 0u ? -INFINITY : ord2f(zi[i]);
+  if (i < (long long)Rp->nx * Rp->ny) zf[i] = zi[i] == 0u ? -INFINITY : ord2f(zi[i]);
 }
 
 // Bilinear height; NaN outside the raster or where no triangle covers a corner.
@@ -310,6 +345,7 @@ __global__ void __launch_bounds__(kLearnBlock)
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long total = (long long)q.cell_count * q.n_pred;
   const bool valid = k < total;
+  const RasterDesc raster = *q.raster;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   float x[kIn];
   int cell = 0, a = 0;
@@ -342,7 +378,7 @@ __global__ void __launch_bounds__(kLearnBlock)
                           0.1875f * sector};
     // Distances: geometric from ~1.5 texels (the local slopes that set most
     // horizons on rough terrain) to dist_search.
-    const float r0 = fminf(fmaxf(1.5f * q.raster.dx, q.dist_search * (1.f / 512.f)),
+    const float r0 = fminf(fmaxf(1.5f * raster.dx, q.dist_search * (1.f / 512.f)),
                            0.5f * q.dist_search);
     const float rstep = __powf(q.dist_search / r0, 1.f / 7.f);
     const double2 cs = __ldg(&q.azim_cs[a]);
@@ -357,7 +393,7 @@ __global__ void __launch_bounds__(kLearnBlock)
 #pragma unroll
       for (int r = 0; r < 8; r++, dist *= rstep) {
         const float dx = dist * hx, dy = dist * hy;
-        const float zt = raster_height(q.raster, Ox + dx, Oy + dy);
+        const float zt = raster_height(raster, Ox + dx, Oy + dy);
         float f = -2.f;  // no terrain
         if (zt == zt) {
           // sin(elevation) of the terrain point seen from O, times 5.
@@ -665,14 +701,15 @@ constexpr size_t kTrainSmem = sizeof(MlpWeights) + sizeof(MlpWeightsT) + sizeof(
 
 }  // namespace
 
-cudaError_t raster_build(const float* vert32, const int* vot, int n_tri, RasterDesc R,
-                         unsigned* zbits, float* z, cudaStream_t s) {
-  const long long n = (long long)R.nx * R.ny;
-  k_raster_fill<<<grid_for(n, 256), 256, 0, s>>>(zbits, n);
+cudaError_t raster_build(const float* vert32, const int* vot, int n_tri, const unsigned* bounds,
+                         long long budget, RasterDesc* rdesc, unsigned* zbits, float* z,
+                         cudaStream_t s) {
+  k_raster_setup<<<1, 1, 0, s>>>(bounds, n_tri, budget, z, rdesc);
+  k_raster_fill<<<grid_for(budget, 256), 256, 0, s>>>(zbits, budget);
   if (n_tri > 0)
-    k_raster_tris<<<grid_for(n_tri, 128), 128, 0, s>>>(vert32, vot, n_tri, R, zbits);
-  k_raster_finish<<<grid_for(n, 256), 256, 0, s>>>(zbits, z, n);
-  note_launches(n_tri > 0 ? 3 : 2);
+    k_raster_tris<<<grid_for(n_tri, 128), 128, 0, s>>>(vert32, vot, n_tri, rdesc, zbits);
+  k_raster_finish<<<grid_for(budget, 256), 256, 0, s>>>(zbits, z, rdesc);
+  note_launches(n_tri > 0 ? 4 : 3);
   return cudaGetLastError();
 }
 

@@ -482,31 +482,16 @@ __device__ __forceinline__ bool visit_node(const Node* __restrict__ nodes, const
 
 // Visits BVH4 node `ref`: continues with the nearest hit child and pushes the
 // other hit children, farthest first; pops when no child is hit. Returns false
-// on stack overflow. kTop > 0: references with kTopFlag name the copies of
-// the tree's top nodes in the block's shared memory (s_top); the others are
-// read from the global tree.
-template <int kTop = 0>
+// on stack overflow.
 __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, const Ray& r,
-                                            int& ref, int* stack, int& sp, StackTop& top,
-                                            const Node4* s_top = nullptr) {
+                                            int& ref, int* stack, int& sp, StackTop& top) {
   // Planes in node order lo.x, hi.x, lo.y, hi.y, lo.z, hi.z: the near plane
   // of an axis is lo + n (n = 1 for a negative inverse direction).
-  float4 nx, fx, ny, fy, nz, fz;
-  int4 ch;
-  if (kTop > 0 && (ref & kTopFlag)) {
-    const Node4* nd = s_top + (ref ^ kTopFlag);
-    const float4* pl = reinterpret_cast<const float4*>(nd);
-    nx = pl[r.nx]; fx = pl[1 - r.nx];
-    ny = pl[2 + r.ny]; fy = pl[3 - r.ny];
-    nz = pl[4 + r.nz]; fz = pl[5 - r.nz];
-    ch = nd->child;
-  } else {
-    const float4* pl = reinterpret_cast<const float4*>(nodes4 + ref);
-    nx = __ldg(pl + r.nx); fx = __ldg(pl + 1 - r.nx);
-    ny = __ldg(pl + 2 + r.ny); fy = __ldg(pl + 3 - r.ny);
-    nz = __ldg(pl + 4 + r.nz); fz = __ldg(pl + 5 - r.nz);
-    ch = __ldg(&nodes4[ref].child);
-  }
+  const float4* pl = reinterpret_cast<const float4*>(nodes4 + ref);
+  const float4 nx = __ldg(pl + r.nx), fx = __ldg(pl + 1 - r.nx);
+  const float4 ny = __ldg(pl + 2 + r.ny), fy = __ldg(pl + 3 - r.ny);
+  const float4 nz = __ldg(pl + 4 + r.nz), fz = __ldg(pl + 5 - r.nz);
+  const int4 ch = __ldg(&nodes4[ref].child);
   float t0, t1, t2, t3;
   int r0 = ch.x, r1 = ch.y, r2 = ch.z, r3 = ch.w;
   if (!(r0 != kEmptyRef && box_hit_nf(r, nx.x, fx.x, ny.x, fy.x, nz.x, fz.x, t0))) t0 = INFINITY;
@@ -822,7 +807,7 @@ struct LaneState {
   __device__ float& f(int k) const { return so[k][t]; }
 };
 
-template <bool kCount, bool kPrecise, bool kWide, int kTop>
+template <bool kCount, bool kPrecise, bool kWide>
 __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     k_trace_warp(const DomainDesc* __restrict__ doms, int ndom, const int* __restrict__ order,
                  int total, int* __restrict__ work, unsigned long long* __restrict__ counters,
@@ -837,21 +822,8 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   __shared__ int si[8][kFlatBlock];
   __shared__ float so[kPrecise ? 6 : 3][kFlatBlock];
   __shared__ int wq[2][kFlatBlock / 32];  // per warp: next and end of its chunk of work ids
-  // kTop > 0 (single-domain calls): the top nodes of the 4-wide tree, copied
-  // into the block's shared memory (dynamic: kTop Node4).
-  extern __shared__ Node4 s_top[];
   constexpr unsigned kFull = 0xffffffffu;
   const int t = threadIdx.x;
-  int root_ref = 0;
-  if (kTop > 0) {
-    const DomainDesc& D0 = doms[0];
-    const int n = D0.top4 ? min(*D0.n_top, kTop) : 0;
-    const float4* src = reinterpret_cast<const float4*>(D0.top4);
-    float4* dst = reinterpret_cast<float4*>(s_top);
-    for (int i = t; i < n * 8; i += kFlatBlock) dst[i] = __ldg(src + i);
-    __syncthreads();
-    root_ref = D0.root == kEmptyRef ? kEmptyRef : (n > 0 ? kTopFlag : D0.root);
-  }
   if ((t & 31) == 0) {
     wq[0][t >> 5] = 0;
     wq[1][t >> 5] = 0;
@@ -979,7 +951,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
                        so[kPrecise ? 3 : 0][t], so[kPrecise ? 4 : 0][t], so[kPrecise ? 5 : 0][t]);
         else
           r = make_ray(so[0][t], so[1][t], so[2][t], d.x, d.y, d.z, D.tfar);
-        ref = kTop > 0 ? root_ref : D.root;
+        ref = D.root;
         sp = 0;
         top.clear();
         pl0 = 0;
@@ -1004,14 +976,11 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     for (int step = 0; step < HZ_NODE_STEPS; step++) {
       if (alive && !need && ref >= 0) {
         if (kCount) nvis++;
-        if (!check_ok(kTop > 0 && (ref & kTopFlag)
-                          ? (ref ^ kTopFlag) < kTop
-                          : ref < (n_tri > 1 ? n_tri - 1 : 1),
-                      kCheckNode, ref, err)) {
+        if (!check_ok(ref < (n_tri > 1 ? n_tri - 1 : 1), kCheckNode, ref, err)) {
           ref = kEmptyRef;  // the ray ends as if it had hit (the call fails)
           need = true;
           last_hit = true;
-        } else if (!(kWide ? visit_node4<kTop>(nodes4, r, ref, stack, sp, top, s_top)
+        } else if (!(kWide ? visit_node4(nodes4, r, ref, stack, sp, top)
                     : visit_node(nodes, r, ref, stack, sp, top))) {
           atomicOr(err, kErrStack);
           need = true;
@@ -1351,7 +1320,7 @@ cudaError_t cell_order(const double* cell_enu, int begin, int count, int id_offs
 // Shared memory is carved out of the SM's 256 KB of L1: ask for just what
 // HZ_WARP_MIN_BLOCKS resident blocks need, so the rest caches the tree.
 template <typename K>
-void prefer_l1(K kernel, size_t dyn_smem = 0) {
+void prefer_l1(K kernel) {
 #if HZ_CARVEOUT
   cudaFuncAttributes fa;
   int dev = 0, smem_sm = 0, reserved = 0;
@@ -1364,8 +1333,7 @@ void prefer_l1(K kernel, size_t dyn_smem = 0) {
     (void)cudaGetLastError();
     return;
   }
-  const long long need =
-      (long long)HZ_WARP_MIN_BLOCKS * ((long long)fa.sharedSizeBytes + (long long)dyn_smem + reserved);
+  const long long need = (long long)HZ_WARP_MIN_BLOCKS * ((long long)fa.sharedSizeBytes + reserved);
   const int pct = (int)std::min<long long>(100, (need * 100 + smem_sm - 1) / smem_sm);
   if (cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct) !=
       cudaSuccess)
@@ -1378,17 +1346,16 @@ void prefer_l1(K kernel, size_t dyn_smem = 0) {
 // One persistent launch: as many blocks as fit on the device at once, at
 // most one block per kFlatBlock work items.
 template <typename... P, typename... A>
-cudaError_t launch_persistent(void (*kernel)(P...), int total, size_t dyn_smem, cudaStream_t s,
-                              A... args) {
+cudaError_t launch_persistent(void (*kernel)(P...), int total, cudaStream_t s, A... args) {
   int dev = 0, sms = 0, per_sm = 0;
-  prefer_l1(kernel, dyn_smem);
+  prefer_l1(kernel);
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kFlatBlock, dyn_smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kFlatBlock, 0);
   long long blocks = (long long)sms * (per_sm > 0 ? per_sm : 1);
   const long long needed = ((long long)total + kFlatBlock - 1) / kFlatBlock;
   if (blocks > needed) blocks = needed;
-  kernel<<<(unsigned)blocks, kFlatBlock, dyn_smem, s>>>(args...);
+  kernel<<<(unsigned)blocks, kFlatBlock, 0, s>>>(args...);
   note_launches(1);
   return cudaGetLastError();
 }
@@ -1396,21 +1363,12 @@ cudaError_t launch_persistent(void (*kernel)(P...), int total, size_t dyn_smem, 
 template <bool kCount, bool kPrecise>
 cudaError_t launch_variant(const DomainDesc* doms, int ndom, const int32_t* order, int total,
                            int* work, unsigned long long* counters, int* err, int advance_min,
-                           int leaf_min, int chunk, int variant, int top_nodes, cudaStream_t s) {
-  if (variant == kTraceWide) {
-    if (!kPrecise && ndom == 1 && top_nodes >= kTopNodesLarge)
-      return launch_persistent(k_trace_warp<kCount, false, true, kTopNodesLarge>, total,
-                               sizeof(Node4) * kTopNodesLarge, s, doms, ndom, order, total,
-                               work, counters, err, advance_min, leaf_min, chunk);
-    if (!kPrecise && ndom == 1 && top_nodes >= kTopNodesSmall)
-      return launch_persistent(k_trace_warp<kCount, false, true, kTopNodesSmall>, total,
-                               sizeof(Node4) * kTopNodesSmall, s, doms, ndom, order, total,
-                               work, counters, err, advance_min, leaf_min, chunk);
-    return launch_persistent(k_trace_warp<kCount, kPrecise, true, 0>, total, 0, s, doms, ndom,
-                             order, total, work, counters, err, advance_min, leaf_min, chunk);
-  }
-  return launch_persistent(k_trace_warp<kCount, kPrecise, false, 0>, total, 0, s, doms, ndom,
-                           order, total, work, counters, err, advance_min, leaf_min, chunk);
+                           int leaf_min, int chunk, int variant, cudaStream_t s) {
+  if (variant == kTraceWide)
+    return launch_persistent(k_trace_warp<kCount, kPrecise, true>, total, s, doms, ndom, order,
+                             total, work, counters, err, advance_min, leaf_min, chunk);
+  return launch_persistent(k_trace_warp<kCount, kPrecise, false>, total, s, doms, ndom, order,
+                           total, work, counters, err, advance_min, leaf_min, chunk);
 }
 
 static cudaError_t launch_search(const DomainDesc* doms, int ndom, const int32_t* order,
@@ -1441,16 +1399,15 @@ static cudaError_t launch_search(const DomainDesc* doms, int ndom, const int32_t
   if (precise)
     return count_work ? launch_variant<true, true>(doms, ndom, order, total, work, counters,
                                                    err, k.advance_min, k.leaf_min, c, k.variant,
-                                                   k.top_nodes, s)
+                                                   s)
                       : launch_variant<false, true>(doms, ndom, order, total, work, counters,
                                                     err, k.advance_min, k.leaf_min, c, k.variant,
-                                                    k.top_nodes, s);
+                                                    s);
   return count_work ? launch_variant<true, false>(doms, ndom, order, total, work, counters, err,
-                                                  k.advance_min, k.leaf_min, c, k.variant,
-                                                  k.top_nodes, s)
+                                                  k.advance_min, k.leaf_min, c, k.variant, s)
                     : launch_variant<false, false>(doms, ndom, order, total, work, counters,
                                                    err, k.advance_min, k.leaf_min, c, k.variant,
-                                                   k.top_nodes, s);
+                                                   s);
 }
 
 cudaError_t trace_rays(const Node* nodes, const Node4* nodes4, const Tri* tris, int root,

@@ -92,7 +92,8 @@ def _check_args(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_t
 def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
              advance_min=0, precision=0, mlp_params=None, raw_index=None, features=None,
              mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0,
-             direct_launch=False, mlp_azimuth_groups=0, start_index=None):
+             direct_launch=False, mlp_azimuth_groups=0, start_index=None,
+             bvh_treelets=False):
     begin, count = (0, 0) if cells is None else (int(cells[0]), int(cells[1]) - int(cells[0]))
     opt = _lib.default_options(device=int(device), count_work=int(bool(count_work)),
                                elev_floor_deg=float(elev_floor_deg),
@@ -101,7 +102,8 @@ def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
                                advance_min=int(advance_min), precision=int(precision),
                                leaf_min=int(leaf_min), leaf_size=int(leaf_size),
                                queue_chunk=int(queue_chunk),
-                               direct_launch=int(bool(direct_launch)))
+                               direct_launch=int(bool(direct_launch)),
+                               bvh_treelets=int(bool(bvh_treelets)))
     if mlp_params is not None:
         p = np.ascontiguousarray(mlp_params, dtype=np.float32)
         if p.size != _lib.load().hz_mlp_num_params():
@@ -128,7 +130,7 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
                         verbose=False, return_stats=False, cells=None, kernel=0,
                         advance_min=0, precision=0, mlp_params=None,
                         mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0,
-                        direct_launch=False, mlp_azimuth_groups=0):
+                        direct_launch=False, mlp_azimuth_groups=0, bvh_treelets=False):
     """Compute the terrain horizon and sky view factor on the GPU.
 
     Arguments and returns as horizon_svf.pyx:15-76: FP64 1-D ``clon, clat``
@@ -141,7 +143,8 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
     persistent search on the binary BVH), its ``advance_min`` / ``leaf_min``
     knobs, the work-queue ``queue_chunk``, the BVH ``leaf_size``,
     ``direct_launch`` (launch each kernel directly instead of replaying the
-    captured CUDA graph of the BVH build and search), the learned warm start
+    captured CUDA graph of the BVH build and search), ``bvh_treelets``
+    (treelet restructuring of the BVH: same results), the learned warm start
     (``mlp_params``; ``mlp_every_azimuth``; ``mlp_azimuth_groups``: search
     items per cell, -1 = chosen by the library, see hz_options) and, with
     ``return_stats``, a third return value with ray counts and phase times.
@@ -172,7 +175,8 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
     opt = _options(device, count_work, elev_floor_deg, verbose, cells, kernel, advance_min,
                    precision, mlp_params, mlp_every_azimuth=mlp_every_azimuth,
                    leaf_min=leaf_min, leaf_size=leaf_size, queue_chunk=queue_chunk,
-                   direct_launch=direct_launch, mlp_azimuth_groups=mlp_azimuth_groups)
+                   direct_launch=direct_launch, mlp_azimuth_groups=mlp_azimuth_groups,
+                   bvh_treelets=bvh_treelets)
     st = _lib.Stats()
     rc = L.hz_horizon_svf(clon.ctypes.data_as(_D), clat.ctypes.data_as(_D),
                           hsurf.ctypes.data_as(_D), vlon.ctypes.data_as(_D),
@@ -194,7 +198,7 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
                             advance_min=0, precision=0, mlp_params=None, raw_index=None,
                             features=None, mlp_every_azimuth=False, leaf_min=0,
                             leaf_size=0, queue_chunk=0, direct_launch=False,
-                            mlp_azimuth_groups=0, start_index=None):
+                            mlp_azimuth_groups=0, start_index=None, bvh_treelets=False):
     """Same computation on CUDA tensors (torch) already resident on one GPU.
 
     Inputs: contiguous float64 / int32 tensors on the same device, layouts as
@@ -240,7 +244,7 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
     opt = _options(dev.index if dev.index is not None else -1, count_work,
                    elev_floor_deg, False, cells, kernel, advance_min, precision, mlp_params,
                    raw_index, features, mlp_every_azimuth, leaf_min, leaf_size, queue_chunk,
-                   direct_launch, mlp_azimuth_groups, start_index)
+                   direct_launch, mlp_azimuth_groups, start_index, bvh_treelets)
     st = _lib.Stats()
     rc = L.hz_horizon_svf_device(clon.data_ptr(), clat.data_ptr(), hsurf.data_ptr(),
                                  vlon.data_ptr(), vlat.data_ptr(),
@@ -316,7 +320,8 @@ def mesh_enu32(clon, clat, hsurf, vlon, vlat, cells_of_vertex, grid_type, device
 def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_deg=-85.0,
                            advance_min=0, return_stats=False, precision=0, mlp_params=None,
                            mlp_every_azimuth=False, kernel=0, leaf_min=0, leaf_size=0,
-                           queue_chunk=0, direct_launch=False, mlp_azimuth_groups=0):
+                           queue_chunk=0, direct_launch=False, mlp_azimuth_groups=0,
+                           bvh_treelets=False):
     """Many independent domains in one call (one persistent search launch).
 
     ``domains``: sequence of ``(inputs, args)`` with ``inputs`` the six arrays
@@ -345,7 +350,8 @@ def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_d
     opt = _options(device, count_work, elev_floor_deg, False, None, kernel, advance_min,
                    precision, mlp_params, mlp_every_azimuth=mlp_every_azimuth,
                    leaf_min=leaf_min, leaf_size=leaf_size, queue_chunk=queue_chunk,
-                   direct_launch=direct_launch, mlp_azimuth_groups=mlp_azimuth_groups)
+                   direct_launch=direct_launch, mlp_azimuth_groups=mlp_azimuth_groups,
+                   bvh_treelets=bvh_treelets)
     st = _lib.Stats()
     rc = _lib.load().hz_horizon_svf_batch(arr, len(structs), 0, None, C.byref(opt),
                                           C.byref(st))

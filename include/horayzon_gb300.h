@@ -95,6 +95,10 @@ typedef struct hz_options {
        item (mlp_azimuth_groups) or at every azimuth (mlp_every_azimuth).
        NULL = not used. */
     const int16_t* start_index;
+    /* 1: restructure the binary BVH by treelets of 5 leaves (Karras & Aila,
+       HPG 2013) before the 4-wide collapse; same results, tree quality
+       only. 0 (default): the plain LBVH. */
+    int32_t bvh_treelets;
 } hz_options;
 
 enum {

@@ -284,6 +284,31 @@ def test_gpu_leaf_size_keeps_results(small_domain, kernel, leaf_size):
     assert st0["num_rays"] == st1["num_rays"]
 
 
+@pytest.mark.parametrize("kernel,leaf_size,precision", [(0, 0, 0), (2, 0, 0), (0, 4, 1),
+                                                       (0, 1, 0)])
+def test_gpu_treelets_keep_results(small_domain, kernel, leaf_size, precision):
+    """Treelet restructuring changes the tree's topology and boxes (every box
+    still the union of the padded leaf boxes), not the rays or hit decisions:
+    same horizons, SVF and ray counts as the plain LBVH, on both trees."""
+    args = (24, 1, 40000.0, 0.2, 1, 2)
+    kw = dict(kernel=kernel, leaf_size=leaf_size, precision=precision, return_stats=True,
+              count_work=True)
+    h0, s0, st0 = horizon_svf_comp_py(*small_domain.inputs(), *args, **kw)
+    h1, s1, st1 = horizon_svf_comp_py(*small_domain.inputs(), *args, bvh_treelets=True, **kw)
+    print("node visits per ray: %.2f plain, %.2f treelets" % (
+        st0["node_visits"] / st0["num_rays"], st1["node_visits"] / st1["num_rays"]))
+    np.testing.assert_array_equal(h0, h1)
+    np.testing.assert_allclose(s0, s1, rtol=0, atol=1e-12)
+    assert st0["num_rays"] == st1["num_rays"]
+
+
+@pytest.mark.parametrize("name", ["g1_n24_r1_svf2", "g0_n24_r1_svf0"])
+def test_gpu_treelets_match_reference_golden(name):
+    g = load_golden(name)
+    h, s = horizon_svf_comp_py(*g["inputs"], *g["args"], bvh_treelets=True)
+    assert_parity(h, s, g["horizon"], g["skyview"])
+
+
 def test_gpu_autotune_picks_a_grid_setting(small_domain, tmp_path, monkeypatch):
     torch = pytest.importorskip("torch")
     from horayzon_extpar_gb300 import autotune, horizon_svf_comp_device
