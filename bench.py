@@ -302,10 +302,15 @@ def auto_groups(ncell: int, nhori: int) -> int:
 # (option elev_floor_deg; reported beside the reference's walk).
 FAST_FLOOR_DEG = -0.25
 
+# The walk below the clip by doubling and bisection (elev_walk 1): the same
+# stop as the step walk wherever visibility is monotone in elevation.
+BISECT = dict(elev_walk=1)
+
 LEARNED_MODES = {"first_azimuth": dict(),
                  "every_azimuth": dict(mlp_every_azimuth=True),
                  "azimuth_groups_auto": dict(mlp_azimuth_groups=-1),
-                 "first_azimuth_fast_floor": dict(elev_floor_deg=FAST_FLOOR_DEG)}
+                 "first_azimuth_fast_floor": dict(elev_floor_deg=FAST_FLOOR_DEG),
+                 "first_azimuth_bisect_walk": dict(BISECT)}
 
 
 def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args, sample=None):
@@ -323,6 +328,7 @@ def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args, sample=None)
     evals = dom.ncell * ARGS[0]
     modes = dict(LEARNED_MODES)
     modes["plain_fast_floor"] = dict(elev_floor_deg=FAST_FLOOR_DEG)
+    modes["plain_bisect_walk"] = dict(BISECT)
     for mode, kw in modes.items():
         if not mode.startswith("plain"):
             kw = dict(kw, mlp_params=params)
@@ -380,7 +386,9 @@ def learned_small_report(stream, reps=5, parity_cells=20000):
         ff = dict(elev_floor_deg=FAST_FLOOR_DEG)
         modes = {"plain": None, "first_azimuth": {}, "azimuth_groups_auto":
                  {"mlp_azimuth_groups": -1}, "plain_fast_floor": ff,
-                 "azimuth_groups_auto_fast_floor": dict(ff, mlp_azimuth_groups=-1)}
+                 "azimuth_groups_auto_fast_floor": dict(ff, mlp_azimuth_groups=-1),
+                 "plain_bisect_walk": dict(BISECT),
+                 "azimuth_groups_auto_bisect_walk": dict(BISECT, mlp_azimuth_groups=-1)}
         sample = oracle_sample(d, ARGS, parity_cells) if parity_cells > 0 else None
         for mode, kw in modes.items():
             extra = {} if kw is None else (dict(kw) if mode.startswith("plain") else
@@ -403,8 +411,11 @@ def learned_small_report(stream, reps=5, parity_cells=20000):
         for mode, base in (("first_azimuth", "plain"), ("azimuth_groups_auto", "plain"),
                            ("plain_fast_floor", "plain"),
                            ("azimuth_groups_auto_fast_floor", "plain"),
-                           ("azimuth_groups_auto_fast_floor", "plain_fast_floor")):
-            tag = "" if base == "plain" else "_fast_floor"
+                           ("azimuth_groups_auto_fast_floor", "plain_fast_floor"),
+                           ("plain_bisect_walk", "plain"),
+                           ("azimuth_groups_auto_bisect_walk", "plain"),
+                           ("azimuth_groups_auto_bisect_walk", "plain_bisect_walk")):
+            tag = base[len("plain"):]
             res[mode]["speedup_vs_plain%s_search" % tag] = (res[base]["search_ms"] /
                                                             res[mode]["search_ms"])
             res[mode]["speedup_vs_plain%s_call" % tag] = (res[base]["call_ms"] /

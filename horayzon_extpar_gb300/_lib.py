@@ -50,11 +50,13 @@ class Options(C.Structure):
                 ("features", C.c_void_p), ("leaf_min", C.c_int32),
                 ("leaf_size", C.c_int32), ("queue_chunk", C.c_int32),
                 ("direct_launch", C.c_int32), ("mlp_azimuth_groups", C.c_int32),
-                ("start_index", C.c_void_p), ("bvh_treelets", C.c_int32)]
+                ("start_index", C.c_void_p), ("bvh_treelets", C.c_int32),
+                ("elev_walk", C.c_int32)]
 
 
 HZ_KERNEL_PERSISTENT, HZ_KERNEL_PER_CELL, HZ_KERNEL_PERSISTENT_BVH2 = 0, 1, 2
 HZ_PRECISION_REFERENCE, HZ_PRECISION_LOCAL = 0, 1
+HZ_WALK_REFERENCE, HZ_WALK_BISECT = 0, 1
 
 
 class Stats(C.Structure):

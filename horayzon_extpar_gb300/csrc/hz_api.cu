@@ -710,6 +710,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.start_m = opt.mlp_params ? b[d].start_m : opt.start_index;
       D.start_all = opt.mlp_every_azimuth ? 1 : 0;
       D.groups = P.groups;
+      D.deep_walk = opt.elev_walk == HZ_WALK_BISECT ? 1 : 0;
       D.item_begin = total_items;
       D.svf_part = b[d].svf_part;
       D.raw_j = n == 1 ? opt.raw_index : nullptr;
@@ -989,6 +990,10 @@ int run_entry(hz_domain* doms, int n, bool on_device, cudaStream_t user_stream,
     return fail(HZ_ERR_VALUE, "the learned warm start needs the persistent kernel");
   if (opt.kernel < HZ_KERNEL_PERSISTENT || opt.kernel > HZ_KERNEL_PERSISTENT_BVH2)
     return fail(HZ_ERR_VALUE, "unknown kernel %d", opt.kernel);
+  if (opt.elev_walk != HZ_WALK_REFERENCE && opt.elev_walk != HZ_WALK_BISECT)
+    return fail(HZ_ERR_VALUE, "unknown elev_walk %d", opt.elev_walk);
+  if (opt.elev_walk == HZ_WALK_BISECT && opt.kernel == HZ_KERNEL_PER_CELL)
+    return fail(HZ_ERR_VALUE, "HZ_WALK_BISECT needs the persistent kernel");
   const bool wide = opt.kernel != HZ_KERNEL_PER_CELL && trace_variant(opt) == kTraceWide;
   if ((opt.raw_index || opt.features) && (n != 1 || !on_device))
     return fail(HZ_ERR_VALUE, "raw_index / features are outputs of the device entry point");

@@ -164,6 +164,10 @@ struct DomainDesc {
   int groups;
   long long item_begin;       // first search item of this domain (items: groups x cells)
   double* svf_part;           // groups > 1 and refine > 1: [groups][ncell] SVF sums
+  // 1: below the clip (a downward walk at elevation <= hori_acc, whose
+  // further candidates all give a clipped horizon) the walk's stop is found
+  // by doubling and bisection instead of one step per ray.
+  int deep_walk;
   int16_t* raw_j;             // optional output: unclipped horizon j (h = j * 0.25 deg)
   double3 centre, pole;       // Earth centre / North Pole in ENU
   double ray_org_elev, hori_acc, elev_floor;

@@ -372,7 +372,7 @@ constexpr int kFlatBlock = 128;
 #define HZ_NODE4_ORDER 0  // 0: hit children sorted by entry distance; 1: nearest first only
 #endif
 
-enum : int { kPhaseStart = 0, kPhaseFirst = 1, kPhaseUp = 2, kPhaseDown = 3 };
+enum : int { kPhaseStart = 0, kPhaseFirst = 1, kPhaseUp = 2, kPhaseDown = 3, kPhaseDeep = 4 };
 
 #ifndef HZ_CHECKED
 #define HZ_CHECKED 0  // 1: the search checks its indices and records violations (kErrBounds)
@@ -693,8 +693,56 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
         phase = last_hit ? kPhaseUp : kPhaseDown;
         up = 0;
       }
-      const bool step_up = phase == kPhaseUp && last_hit && up < kMaxUpSteps;
-      const bool step_dn = phase == kPhaseDown && !last_hit && elev > D.elev_floor;
+      bool hit = last_hit;
+      if (phase == kPhaseDeep) {
+        // Result of probe k = m0 - m of the search for the highest hit below
+        // the clip (DomainDesc::deep_walk): bracket (lo missed, hi hit), K =
+        // candidates down to the floor (in `up`), m0 and e0 (SV(6)) the
+        // last miss of the step walk.
+        const int K = up, m0 = st.i(9), cur = m0 - m;
+        int lo = st.i(8) & 0xffff, hi = st.i(8) >> 16;
+        if (last_hit) hi = cur;
+        else lo = cur;
+        const int next = hi > K ? (lo >= K ? 0 : min(max(1, 2 * lo), K))  // no hit yet: double
+                                : (hi - lo > 1 ? (lo + hi) >> 1 : 0);     // bisect
+        if (next > 0) {
+          m = m0 - next;
+          st.i(8) = lo | (hi << 16);
+          emit = true;
+          break;
+        }
+        // The walk's stop: the reference's elevation after ks steps of
+        // cpp:538, accumulated as it does.
+        const int ks = hi > K ? K : hi;
+        hit = hi <= K;
+        for (int q = 0; q < ks; q++) elev -= D.two_ha;
+        m = m0 - ks;
+        SV(6) = elev;
+        phase = kPhaseDown;
+      }
+      const bool step_up = phase == kPhaseUp && hit && up < kMaxUpSteps;
+      const bool step_dn = phase == kPhaseDown && !hit && elev > D.elev_floor;
+      if (step_dn && D.deep_walk && elev <= ha) {
+        // Every further candidate e_k = e0 - k 2 hori_acc gives a horizon
+        // e_k + hori_acc <= 0, clipped to 0 (cpp:737-741): the walk only
+        // decides the elevation carried into the next azimuth, its first
+        // hit. Doubling steps then bisection find it in O(log K) rays; where
+        // hits are contiguous below that stop (visibility monotone in
+        // elevation) it is the step walk's stop.
+        int K = 0;
+        double e = elev;
+        do {
+          e -= D.two_ha;
+          K++;
+        } while (e > D.elev_floor);
+        up = K;
+        st.i(9) = m;
+        st.i(8) = (K + 1) << 16;
+        phase = kPhaseDeep;
+        m--;  // probe k = 1
+        emit = true;
+        break;
+      }
       if (step_up || step_dn) {
         if (step_up) {
           up++;
@@ -812,14 +860,15 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
     k_trace_warp(const DomainDesc* __restrict__ doms, int ndom, const int* __restrict__ order,
                  int total, int* __restrict__ work, unsigned long long* __restrict__ counters,
                  int* __restrict__ err, int advance_min, int leaf_min, int chunk) {
-  // Per-lane search state (116 bytes; the rest of the SM's L1 caches the
+  // Per-lane search state (124 bytes; the rest of the SM's L1 caches the
   // tree). FP64: 0-2 sphere normal U, 3-5 horizontal direction of the
   // current azimuth, 6 elevation accumulator, 7 sector sum, 8 SVF sum.
   // Integers: domain, cell, azimuth, phase, upward steps, lattice index m of
   // the current elevation, position of the cell in the work order, end
-  // azimuth of the item. FP32 ray origin (hi, and lo in precise mode).
+  // azimuth of the item, and the deep walk's bracket and start. FP32 ray
+  // origin (hi, and lo in precise mode).
   __shared__ double sv[9][kFlatBlock];
-  __shared__ int si[8][kFlatBlock];
+  __shared__ int si[10][kFlatBlock];
   __shared__ float so[kPrecise ? 6 : 3][kFlatBlock];
   __shared__ int wq[2][kFlatBlock / 32];  // per warp: next and end of its chunk of work ids
   constexpr unsigned kFull = 0xffffffffu;
@@ -830,7 +879,7 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
   }
   __syncwarp();
 #pragma unroll
-  for (int q = 0; q < 8; q++) si[q][t] = 0;
+  for (int q = 0; q < 10; q++) si[q][t] = 0;
   si[3][t] = kPhaseStart;
 
   bool alive = true, need = true, last_hit = false;

@@ -93,7 +93,7 @@ def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
              advance_min=0, precision=0, mlp_params=None, raw_index=None, features=None,
              mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0,
              direct_launch=False, mlp_azimuth_groups=0, start_index=None,
-             bvh_treelets=False):
+             bvh_treelets=False, elev_walk=0):
     begin, count = (0, 0) if cells is None else (int(cells[0]), int(cells[1]) - int(cells[0]))
     opt = _lib.default_options(device=int(device), count_work=int(bool(count_work)),
                                elev_floor_deg=float(elev_floor_deg),
@@ -103,7 +103,8 @@ def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
                                leaf_min=int(leaf_min), leaf_size=int(leaf_size),
                                queue_chunk=int(queue_chunk),
                                direct_launch=int(bool(direct_launch)),
-                               bvh_treelets=int(bool(bvh_treelets)))
+                               bvh_treelets=int(bool(bvh_treelets)),
+                               elev_walk=int(elev_walk))
     if mlp_params is not None:
         p = np.ascontiguousarray(mlp_params, dtype=np.float32)
         if p.size != _lib.load().hz_mlp_num_params():
@@ -130,7 +131,8 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
                         verbose=False, return_stats=False, cells=None, kernel=0,
                         advance_min=0, precision=0, mlp_params=None,
                         mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0,
-                        direct_launch=False, mlp_azimuth_groups=0, bvh_treelets=False):
+                        direct_launch=False, mlp_azimuth_groups=0, bvh_treelets=False,
+                        elev_walk=0):
     """Compute the terrain horizon and sky view factor on the GPU.
 
     Arguments and returns as horizon_svf.pyx:15-76: FP64 1-D ``clon, clat``
@@ -144,7 +146,9 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
     knobs, the work-queue ``queue_chunk``, the BVH ``leaf_size``,
     ``direct_launch`` (launch each kernel directly instead of replaying the
     captured CUDA graph of the BVH build and search), ``bvh_treelets``
-    (treelet restructuring of the BVH: same results), the learned warm start
+    (treelet restructuring of the BVH: same results), ``elev_walk`` (1:
+    bisection for the downward walk below the clip, see hz_options), the
+    learned warm start
     (``mlp_params``; ``mlp_every_azimuth``; ``mlp_azimuth_groups``: search
     items per cell, -1 = chosen by the library, see hz_options) and, with
     ``return_stats``, a third return value with ray counts and phase times.
@@ -176,7 +180,7 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
                    precision, mlp_params, mlp_every_azimuth=mlp_every_azimuth,
                    leaf_min=leaf_min, leaf_size=leaf_size, queue_chunk=queue_chunk,
                    direct_launch=direct_launch, mlp_azimuth_groups=mlp_azimuth_groups,
-                   bvh_treelets=bvh_treelets)
+                   bvh_treelets=bvh_treelets, elev_walk=elev_walk)
     st = _lib.Stats()
     rc = L.hz_horizon_svf(clon.ctypes.data_as(_D), clat.ctypes.data_as(_D),
                           hsurf.ctypes.data_as(_D), vlon.ctypes.data_as(_D),
@@ -198,7 +202,8 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
                             advance_min=0, precision=0, mlp_params=None, raw_index=None,
                             features=None, mlp_every_azimuth=False, leaf_min=0,
                             leaf_size=0, queue_chunk=0, direct_launch=False,
-                            mlp_azimuth_groups=0, start_index=None, bvh_treelets=False):
+                            mlp_azimuth_groups=0, start_index=None, bvh_treelets=False,
+                            elev_walk=0):
     """Same computation on CUDA tensors (torch) already resident on one GPU.
 
     Inputs: contiguous float64 / int32 tensors on the same device, layouts as
@@ -244,7 +249,7 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
     opt = _options(dev.index if dev.index is not None else -1, count_work,
                    elev_floor_deg, False, cells, kernel, advance_min, precision, mlp_params,
                    raw_index, features, mlp_every_azimuth, leaf_min, leaf_size, queue_chunk,
-                   direct_launch, mlp_azimuth_groups, start_index, bvh_treelets)
+                   direct_launch, mlp_azimuth_groups, start_index, bvh_treelets, elev_walk)
     st = _lib.Stats()
     rc = L.hz_horizon_svf_device(clon.data_ptr(), clat.data_ptr(), hsurf.data_ptr(),
                                  vlon.data_ptr(), vlat.data_ptr(),
@@ -321,7 +326,7 @@ def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_d
                            advance_min=0, return_stats=False, precision=0, mlp_params=None,
                            mlp_every_azimuth=False, kernel=0, leaf_min=0, leaf_size=0,
                            queue_chunk=0, direct_launch=False, mlp_azimuth_groups=0,
-                           bvh_treelets=False):
+                           bvh_treelets=False, elev_walk=0):
     """Many independent domains in one call (one persistent search launch).
 
     ``domains``: sequence of ``(inputs, args)`` with ``inputs`` the six arrays
@@ -351,7 +356,7 @@ def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_d
                    precision, mlp_params, mlp_every_azimuth=mlp_every_azimuth,
                    leaf_min=leaf_min, leaf_size=leaf_size, queue_chunk=queue_chunk,
                    direct_launch=direct_launch, mlp_azimuth_groups=mlp_azimuth_groups,
-                   bvh_treelets=bvh_treelets)
+                   bvh_treelets=bvh_treelets, elev_walk=elev_walk)
     st = _lib.Stats()
     rc = _lib.load().hz_horizon_svf_batch(arr, len(structs), 0, None, C.byref(opt),
                                           C.byref(st))

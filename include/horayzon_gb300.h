@@ -99,7 +99,22 @@ typedef struct hz_options {
        HPG 2013) before the 4-wide collapse; same results, tree quality
        only. 0 (default): the plain LBVH. */
     int32_t bvh_treelets;
+    /* The downward elevation walk (mo_lradtopo_horayzon.cpp:536-547) once it
+       is at or below +0.25 deg, where every further step gives a horizon
+       clipped to 0 and only decides the elevation carried into the next
+       azimuth: HZ_WALK_REFERENCE (default) one step per ray as the
+       reference; HZ_WALK_BISECT doubling steps then bisection for the same
+       stop, which it finds wherever the rays below it hit and those above
+       it miss (visibility monotone in elevation) -- then the outputs are the
+       reference's, from fewer rays (hz_stats.num_rays counts the rays cast).
+       Persistent kernel only. */
+    int32_t elev_walk;
 } hz_options;
+
+enum {
+    HZ_WALK_REFERENCE = 0,
+    HZ_WALK_BISECT = 1
+};
 
 enum {
     /* FP32 vertices and ray origins in one global ENU frame, as the reference

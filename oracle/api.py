@@ -23,7 +23,7 @@ class Options(C.Structure):
                 ("cells", _I), ("n_cells", C.c_int),
                 ("elev_floor_deg", C.c_double), ("brute_force", C.c_int),
                 ("start_m", C.POINTER(C.c_int16)), ("groups", C.c_int),
-                ("start_all", C.c_int)]
+                ("start_all", C.c_int), ("bisect_walk", C.c_int)]
 
 
 class Result(C.Structure):
@@ -102,13 +102,15 @@ def _p(a, t):
 def horizon_svf(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_type,
                 dist_search, ray_org_elev, refine_factor, svf_type, *, precision=0,
                 nthreads=0, cells=None, elev_floor_deg=-85.0, brute_force=False,
-                start_index=None, groups=1, start_all=False):
+                start_index=None, groups=1, start_all=False, bisect_walk=False):
     """Oracle horizon [nhori, ncell] (deg), skyview [ncell], stats dict.
 
     With ``cells`` only those columns/entries are computed (others are NaN).
     ``start_index`` (int16 [L, ncell], L = num_hori * refine_factor): warm
     start lattice indices; each cell's azimuths form ``groups`` runs whose
     first azimuth starts there (every azimuth with ``start_all``).
+    ``bisect_walk``: the downward walk below the clip by doubling and
+    bisection (the GPU library's HZ_WALK_BISECT).
     """
     clon, clat, hsurf, vlon, vlat = map(_f64, (clon, clat, hsurf, vlon, vlat))
     cov = _i32(cells_of_vertex)
@@ -116,7 +118,8 @@ def horizon_svf(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori, grid_t
     horizon = np.full((num_hori, ncell), np.nan)
     skyview = np.full(ncell, np.nan)
     opt = Options(precision=precision, nthreads=nthreads, cells=None, n_cells=0,
-                  elev_floor_deg=elev_floor_deg, brute_force=int(brute_force))
+                  elev_floor_deg=elev_floor_deg, brute_force=int(brute_force),
+                  bisect_walk=int(bool(bisect_walk)))
     if cells is not None:
         cells = _i32(cells)
         opt.cells = _p(cells, _I)

@@ -253,7 +253,7 @@ typedef struct {
     const int32_t* cells;
     int n_work;
     const int16_t* start_m;
-    int groups, start_all;
+    int groups, start_all, bisect_walk;
     atomic_int next;
     /* per-run totals */
     atomic_llong rays, nodes, tris, overflow;
@@ -333,11 +333,42 @@ static int64_t trace_cell(const trace_job* J, int i, hzo_counts* cnt) {
             }
             h = elev - ha;
         } else {
-            while ((!hit) && (elev > J->elev_floor)) {
+            /* With bisect_walk the step walk stops at the clip (elev <= ha),
+             * where every further candidate's horizon is clipped to 0. */
+            while ((!hit) && (elev > J->elev_floor) && !(J->bisect_walk && elev <= ha)) {
                 elev -= (2.0 * ha);
                 dir = rotate3(dir, axis, -J->elev_sin_2ha, J->elev_cos_2ha);
                 hit = cast_ray(J, &o64, o32, dir, cnt);
                 rays++;
+            }
+            if (!hit && elev > J->elev_floor) {
+                /* The stop of the step walk from e0 = elev: the first k with
+                 * a hit, or K (the first step at or below the floor). Probe
+                 * k = 1, 2, 4, ... then bisect; the direction of step k is
+                 * the step walk's, k incremental rotations from e0. */
+                int K = 0;
+                double e = elev;
+                do {
+                    e -= (2.0 * ha);
+                    K++;
+                } while (e > J->elev_floor);
+                const v3d d0 = dir;
+                int lo = 0, hi = K + 1, next = 1;
+                while (next > 0) {
+                    v3d d = d0;
+                    for (int q = 0; q < next; q++)
+                        d = rotate3(d, axis, -J->elev_sin_2ha, J->elev_cos_2ha);
+                    if (cast_ray(J, &o64, o32, d, cnt)) hi = next;
+                    else lo = next;
+                    rays++;
+                    if (hi > K) next = lo >= K ? 0 : (2 * lo > K ? K : (2 * lo < 1 ? 1 : 2 * lo));
+                    else next = hi - lo > 1 ? (lo + hi) / 2 : 0;
+                }
+                const int ks = hi > K ? K : hi;
+                for (int q = 0; q < ks; q++) {
+                    elev -= (2.0 * ha);
+                    dir = rotate3(dir, axis, -J->elev_sin_2ha, J->elev_cos_2ha);
+                }
             }
             h = elev + ha;
         }
@@ -460,6 +491,7 @@ int hzo_horizon_svf(const double* clon, const double* clat, const double* hsurf,
     J.start_m = opt.start_m;
     J.groups = opt.groups;
     J.start_all = opt.start_all;
+    J.bisect_walk = opt.bisect_walk;
     if (J.start_m && J.groups > 1 && (nhori % J.groups) != 0) {
         free(enu);
         return -1;

@@ -30,6 +30,11 @@ typedef struct {
     const int16_t* start_m;
     int groups;
     int start_all;
+    /* 1: the GPU library's HZ_WALK_BISECT: a downward walk at or below the
+       clip (elevation <= hori_acc) finds its stop by doubling steps then
+       bisection, the rays at intermediate steps rotated but not cast; 0 =
+       the reference's step walk. */
+    int bisect_walk;
 } hzo_options;
 
 typedef struct {
