@@ -374,6 +374,22 @@ constexpr int kFlatBlock = 128;
 
 enum : int { kPhaseStart = 0, kPhaseFirst = 1, kPhaseUp = 2, kPhaseDown = 3, kPhaseDeep = 4 };
 
+// Bracket sentinel of the walk below the clip: no hit found yet.
+constexpr int kNoHit = 0x7fff;
+
+// Candidates of the downward step walk from e0 down to the floor (cpp:538):
+// the k of the first e_k = e0 - 2 hori_acc - ... - 2 hori_acc <= elev_floor,
+// accumulated as the reference does.
+__device__ __forceinline__ int deep_walk_count(double e0, const DomainDesc& D) {
+  int K = 0;
+  double e = e0;
+  do {
+    e -= D.two_ha;
+    K++;
+  } while (e > D.elev_floor);
+  return K;
+}
+
 #ifndef HZ_CHECKED
 #define HZ_CHECKED 0  // 1: the search checks its indices and records violations (kErrBounds)
 #endif
@@ -696,14 +712,18 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
       bool hit = last_hit;
       if (phase == kPhaseDeep) {
         // Result of probe k = m0 - m of the search for the highest hit below
-        // the clip (DomainDesc::deep_walk): bracket (lo missed, hi hit), K =
-        // candidates down to the floor (in `up`), m0 and e0 (SV(6)) the
-        // last miss of the step walk.
-        const int K = up, m0 = st.i(9), cur = m0 - m;
+        // the clip (DomainDesc::deep_walk): bracket (lo missed, hi hit; hi =
+        // kNoHit before the first hit), m0 and e0 (SV(6)) the last miss of
+        // the step walk, `up` the number K of candidates down to the floor
+        // (negative while it is only the estimate -K').
+        const int m0 = st.i(9), cur = m0 - m;
         int lo = st.i(8) & 0xffff, hi = st.i(8) >> 16;
         if (last_hit) hi = cur;
         else lo = cur;
-        const int next = hi > K ? (lo >= K ? 0 : min(max(1, 2 * lo), K))  // no hit yet: double
+        const bool no_hit = hi == kNoHit;
+        if (no_hit && up < 0 && 2 * lo >= -up - 2) up = deep_walk_count(elev, D);
+        const int K = up < 0 ? -up : up;
+        const int next = no_hit ? (lo >= K ? 0 : min(max(1, 2 * lo), K))  // double
                                 : (hi - lo > 1 ? (lo + hi) >> 1 : 0);     // bisect
         if (next > 0) {
           m = m0 - next;
@@ -713,8 +733,8 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
         }
         // The walk's stop: the reference's elevation after ks steps of
         // cpp:538, accumulated as it does.
-        const int ks = hi > K ? K : hi;
-        hit = hi <= K;
+        const int ks = no_hit ? K : hi;
+        hit = !no_hit;
         for (int q = 0; q < ks; q++) elev -= D.two_ha;
         m = m0 - ks;
         SV(6) = elev;
@@ -729,15 +749,12 @@ __device__ __forceinline__ int search_step(const S& st, const DomainDesc* __rest
         // hit. Doubling steps then bisection find it in O(log K) rays; where
         // hits are contiguous below that stop (visibility monotone in
         // elevation) it is the step walk's stop.
-        int K = 0;
-        double e = elev;
-        do {
-          e -= D.two_ha;
-          K++;
-        } while (e > D.elev_floor);
-        up = K;
+        // K is estimated here (within one of the count); the exact count,
+        // a serial FP64 accumulation, runs only once the doubling comes
+        // within two candidates of the floor.
+        up = -(int)ceilf((float)(elev - D.elev_floor) / (float)D.two_ha);
         st.i(9) = m;
-        st.i(8) = (K + 1) << 16;
+        st.i(8) = kNoHit << 16;
         phase = kPhaseDeep;
         m--;  // probe k = 1
         emit = true;
