@@ -51,7 +51,7 @@ class Options(C.Structure):
                 ("leaf_size", C.c_int32), ("queue_chunk", C.c_int32),
                 ("direct_launch", C.c_int32), ("mlp_azimuth_groups", C.c_int32),
                 ("start_index", C.c_void_p), ("bvh_treelets", C.c_int32),
-                ("elev_walk", C.c_int32)]
+                ("elev_walk", C.c_int32), ("occluder_cache", C.c_int32)]
 
 
 HZ_KERNEL_PERSISTENT, HZ_KERNEL_PER_CELL, HZ_KERNEL_PERSISTENT_BVH2 = 0, 1, 2

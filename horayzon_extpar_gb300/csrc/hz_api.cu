@@ -711,6 +711,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.start_all = opt.mlp_every_azimuth ? 1 : 0;
       D.groups = P.groups;
       D.deep_walk = opt.elev_walk == HZ_WALK_BISECT ? 1 : 0;
+      D.occ_cache = opt.occluder_cache != 0 ? 1 : 0;
       D.item_begin = total_items;
       D.svf_part = b[d].svf_part;
       D.raw_j = n == 1 ? opt.raw_index : nullptr;
@@ -1131,6 +1132,7 @@ void hz_default_options(hz_options* opt) {
   opt->size = sizeof(hz_options);
   opt->device = -1;
   opt->elev_floor_deg = -85.0;
+  opt->occluder_cache = 1;
 }
 
 const char* hz_last_error(void) { return g_last_error.c_str(); }

@@ -168,6 +168,9 @@ struct DomainDesc {
   // further candidates all give a clipped horizon) the walk's stop is found
   // by doubling and bisection instead of one step per ray.
   int deep_walk;
+  // 1: an upward step first tests the triangle that hid the step below
+  // (k_trace_warp's occluder cache; same results, fewer traversals).
+  int occ_cache;
   int16_t* raw_j;             // optional output: unclipped horizon j (h = j * 0.25 deg)
   double3 centre, pole;       // Earth centre / North Pole in ENU
   double ray_org_elev, hori_acc, elev_floor;

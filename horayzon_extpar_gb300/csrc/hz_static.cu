@@ -275,6 +275,7 @@ extern "C" int hz_horizon_svf_device_static(
   D.cell_offset = 0;
   D.groups = 1;
   D.item_begin = 0;
+  D.occ_cache = 1;
   D.root = n_tri > 0 ? 0 : kEmptyRef;
   D.n_tri = n_tri;
   D.ncell = num_cell;

@@ -93,7 +93,7 @@ def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
              advance_min=0, precision=0, mlp_params=None, raw_index=None, features=None,
              mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0,
              direct_launch=False, mlp_azimuth_groups=0, start_index=None,
-             bvh_treelets=False, elev_walk=0):
+             bvh_treelets=False, elev_walk=0, occluder_cache=True):
     begin, count = (0, 0) if cells is None else (int(cells[0]), int(cells[1]) - int(cells[0]))
     opt = _lib.default_options(device=int(device), count_work=int(bool(count_work)),
                                elev_floor_deg=float(elev_floor_deg),
@@ -104,7 +104,8 @@ def _options(device, count_work, elev_floor_deg, verbose, cells=None, kernel=0,
                                queue_chunk=int(queue_chunk),
                                direct_launch=int(bool(direct_launch)),
                                bvh_treelets=int(bool(bvh_treelets)),
-                               elev_walk=int(elev_walk))
+                               elev_walk=int(elev_walk),
+                               occluder_cache=int(bool(occluder_cache)))
     if mlp_params is not None:
         p = np.ascontiguousarray(mlp_params, dtype=np.float32)
         if p.size != _lib.load().hz_mlp_num_params():
@@ -132,7 +133,7 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
                         advance_min=0, precision=0, mlp_params=None,
                         mlp_every_azimuth=False, leaf_min=0, leaf_size=0, queue_chunk=0,
                         direct_launch=False, mlp_azimuth_groups=0, bvh_treelets=False,
-                        elev_walk=0):
+                        elev_walk=0, occluder_cache=True):
     """Compute the terrain horizon and sky view factor on the GPU.
 
     Arguments and returns as horizon_svf.pyx:15-76: FP64 1-D ``clon, clat``
@@ -147,7 +148,9 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
     ``direct_launch`` (launch each kernel directly instead of replaying the
     captured CUDA graph of the BVH build and search), ``bvh_treelets``
     (treelet restructuring of the BVH: same results), ``elev_walk`` (1:
-    bisection for the downward walk below the clip, see hz_options), the
+    bisection for the downward walk below the clip, see hz_options),
+    ``occluder_cache`` (False: traverse the tree for every ray; same
+    results), the
     learned warm start
     (``mlp_params``; ``mlp_every_azimuth``; ``mlp_azimuth_groups``: search
     items per cell, -1 = chosen by the library, see hz_options) and, with
@@ -180,7 +183,8 @@ def horizon_svf_comp_py(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_hori
                    precision, mlp_params, mlp_every_azimuth=mlp_every_azimuth,
                    leaf_min=leaf_min, leaf_size=leaf_size, queue_chunk=queue_chunk,
                    direct_launch=direct_launch, mlp_azimuth_groups=mlp_azimuth_groups,
-                   bvh_treelets=bvh_treelets, elev_walk=elev_walk)
+                   bvh_treelets=bvh_treelets, elev_walk=elev_walk,
+                   occluder_cache=occluder_cache)
     st = _lib.Stats()
     rc = L.hz_horizon_svf(clon.ctypes.data_as(_D), clat.ctypes.data_as(_D),
                           hsurf.ctypes.data_as(_D), vlon.ctypes.data_as(_D),
@@ -203,7 +207,7 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
                             features=None, mlp_every_azimuth=False, leaf_min=0,
                             leaf_size=0, queue_chunk=0, direct_launch=False,
                             mlp_azimuth_groups=0, start_index=None, bvh_treelets=False,
-                            elev_walk=0):
+                            elev_walk=0, occluder_cache=True):
     """Same computation on CUDA tensors (torch) already resident on one GPU.
 
     Inputs: contiguous float64 / int32 tensors on the same device, layouts as
@@ -249,7 +253,8 @@ def horizon_svf_comp_device(clon, clat, hsurf, vlon, vlat, cells_of_vertex, num_
     opt = _options(dev.index if dev.index is not None else -1, count_work,
                    elev_floor_deg, False, cells, kernel, advance_min, precision, mlp_params,
                    raw_index, features, mlp_every_azimuth, leaf_min, leaf_size, queue_chunk,
-                   direct_launch, mlp_azimuth_groups, start_index, bvh_treelets, elev_walk)
+                   direct_launch, mlp_azimuth_groups, start_index, bvh_treelets, elev_walk,
+                   occluder_cache)
     st = _lib.Stats()
     rc = L.hz_horizon_svf_device(clon.data_ptr(), clat.data_ptr(), hsurf.data_ptr(),
                                  vlon.data_ptr(), vlat.data_ptr(),
@@ -326,7 +331,7 @@ def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_d
                            advance_min=0, return_stats=False, precision=0, mlp_params=None,
                            mlp_every_azimuth=False, kernel=0, leaf_min=0, leaf_size=0,
                            queue_chunk=0, direct_launch=False, mlp_azimuth_groups=0,
-                           bvh_treelets=False, elev_walk=0):
+                           bvh_treelets=False, elev_walk=0, occluder_cache=True):
     """Many independent domains in one call (one persistent search launch).
 
     ``domains``: sequence of ``(inputs, args)`` with ``inputs`` the six arrays
@@ -356,7 +361,8 @@ def horizon_svf_comp_batch(domains, *, device=-1, count_work=False, elev_floor_d
                    precision, mlp_params, mlp_every_azimuth=mlp_every_azimuth,
                    leaf_min=leaf_min, leaf_size=leaf_size, queue_chunk=queue_chunk,
                    direct_launch=direct_launch, mlp_azimuth_groups=mlp_azimuth_groups,
-                   bvh_treelets=bvh_treelets, elev_walk=elev_walk)
+                   bvh_treelets=bvh_treelets, elev_walk=elev_walk,
+                   occluder_cache=occluder_cache)
     st = _lib.Stats()
     rc = _lib.load().hz_horizon_svf_batch(arr, len(structs), 0, None, C.byref(opt),
                                           C.byref(st))

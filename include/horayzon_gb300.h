@@ -109,6 +109,12 @@ typedef struct hz_options {
        reference's, from fewer rays (hz_stats.num_rays counts the rays cast).
        Persistent kernel only. */
     int32_t elev_walk;
+    /* 1 (default): an upward step of the elevation walk first tests the
+       triangle that hid the ray one step below; the query is any-hit, so a
+       hit there is the full traversal's answer and the tree is not
+       traversed for that ray. Same results, same ray count; 0 traverses
+       every ray. Persistent kernels; the per-cell kernel ignores it. */
+    int32_t occluder_cache;
 } hz_options;
 
 enum {
