@@ -369,7 +369,7 @@ constexpr int kFlatBlock = 128;
 #define HZ_NODE_STEPS 2  // node visits per lane in one node pass
 #endif
 #ifndef HZ_NODE4_ORDER
-#define HZ_NODE4_ORDER 0  // 0: hit children sorted by entry distance; 1: nearest first only
+#define HZ_NODE4_ORDER 1  // 0: hit children sorted by entry distance; 1: nearest first only
 #endif
 
 enum : int { kPhaseStart = 0, kPhaseFirst = 1, kPhaseUp = 2, kPhaseDown = 3, kPhaseDeep = 4 };
