@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 from horayzon_extpar_gb300 import _lib, horizon_svf_comp_py, synthetic
+from horayzon_extpar_gb300.horizon_svf import horizon_svf_comp_batch
 
 pytestmark = pytest.mark.gpu
 
@@ -45,7 +46,6 @@ def test_occluder_cache_keeps_results_and_ray_count(name, kw, args, extra):
 
 def test_occluder_cache_in_a_batch():
     doms = [(_domain(kw).inputs(), args) for _, kw, args, _ in CASES[:2]]
-    from horayzon_extpar_gb300 import horizon_svf_comp_batch
     off = horizon_svf_comp_batch(doms, occluder_cache=False)
     on = horizon_svf_comp_batch(doms)
     for (h0, s0), (h1, s1) in zip(off, on):
