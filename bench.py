@@ -742,7 +742,10 @@ def run_gpu(args):
                      "bvh": float(np.mean([s["ms_bvh"] for s in stats])),
                      "trace": trace_ms},
         "e2e": {"value": world * evals / e2e_s, "unit": "evals/s",
-                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "wall_ms_per_step": 1e3 * e2e_s,
+                "phase_ms_last_step": {k: float(getattr(st, k)) for k in (
+                    "ms_h2d", "ms_mesh", "ms_bvh", "ms_trace", "ms_d2h")}},
         # The search reads its tree and triangles mostly from L1 / L2 (DRAM
         # traffic is ~2 % of the algorithmic bytes): `frac` is the HBM-
         # equivalent fraction of the measured copy bandwidth, `l2_frac` the
