@@ -35,8 +35,17 @@ struct Ray {
   float pox, poy, poz;    // origin permuted to (kx, ky, kz)
   float plx, ply, plz;    // precise mode: FP32 residual of the origin, permuted
   float Sx, Sy, Sz;       // shear constants
-  int kx, ky, kz;
-  int nx, ny, nz;         // 1 where the inverse direction is negative (near plane = hi)
+  // Axis order of the shear (kx, ky, kz) and the signs of the inverse
+  // direction (n = 1 where negative: near plane = hi), packed in one
+  // register: kx | ky << 2 | kz << 4 | nx << 6 | ny << 7 | nz << 8. The
+  // persistent search then holds its state in 64 registers without spills.
+  unsigned ax;
+  __device__ int kx() const { return ax & 3u; }
+  __device__ int ky() const { return (ax >> 2) & 3u; }
+  __device__ int kz() const { return (ax >> 4) & 3u; }
+  __device__ int nx() const { return (ax >> 6) & 1u; }
+  __device__ int ny() const { return (ax >> 7) & 1u; }
+  __device__ int nz() const { return (ax >> 8) & 1u; }
   float tfar;
 };
 
@@ -51,16 +60,16 @@ __device__ __forceinline__ Ray make_ray(float ox, float oy, float oz, float dx, 
   r.ox = ox; r.oy = oy; r.oz = oz;
   r.ix = __frcp_rn(dx); r.iy = __frcp_rn(dy); r.iz = __frcp_rn(dz);
   r.oix = __fmul_rn(ox, r.ix); r.oiy = __fmul_rn(oy, r.iy); r.oiz = __fmul_rn(oz, r.iz);
-  r.nx = signbit(r.ix) ? 1 : 0;
-  r.ny = signbit(r.iy) ? 1 : 0;
-  r.nz = signbit(r.iz) ? 1 : 0;
+  const unsigned sx = signbit(r.ix) ? 1u : 0u, sy = signbit(r.iy) ? 1u : 0u,
+                 sz = signbit(r.iz) ? 1u : 0u;
   const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
   int kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
   int kx = kz + 1 == 3 ? 0 : kz + 1;
   int ky = kx + 1 == 3 ? 0 : kx + 1;
   const float dkz = sel3(dx, dy, dz, kz);
   if (dkz < 0.f) { int tmp = kx; kx = ky; ky = tmp; }
-  r.kx = kx; r.ky = ky; r.kz = kz;
+  r.ax = (unsigned)kx | ((unsigned)ky << 2) | ((unsigned)kz << 4) | (sx << 6) | (sy << 7) |
+         (sz << 8);
   r.Sx = __fdiv_rn(sel3(dx, dy, dz, kx), dkz);
   r.Sy = __fdiv_rn(sel3(dx, dy, dz, ky), dkz);
   r.Sz = __frcp_rn(dkz);
@@ -147,9 +156,9 @@ __device__ __forceinline__ bool tri_hit_hl(const Ray& r, const float4 X, const f
 __device__ __forceinline__ void load_tri(const Tri* __restrict__ tris, const Ray& r, int k,
                                          float4& X, float4& Y, float4& Z) {
   const float4* t = reinterpret_cast<const float4*>(tris + k);
-  X = __ldg(t + r.kx);
-  Y = __ldg(t + r.ky);
-  Z = __ldg(t + r.kz);
+  X = __ldg(t + r.kx());
+  Y = __ldg(t + r.ky());
+  Z = __ldg(t + r.kz());
 }
 
 // Conservative slab test: the boxes carry a margin far above the rounding of
@@ -174,8 +183,8 @@ __device__ __forceinline__ bool box_hit_nf(const Ray& r, float nx, float fx, flo
 // The same test on a box given as (lo, hi) per axis.
 __device__ __forceinline__ bool box_hit(const Ray& r, float lx, float hx, float ly, float hy,
                                         float lz, float hz, float& tentry) {
-  return box_hit_nf(r, r.nx ? hx : lx, r.nx ? lx : hx, r.ny ? hy : ly, r.ny ? ly : hy,
-                    r.nz ? hz : lz, r.nz ? lz : hz, tentry);
+  return box_hit_nf(r, r.nx() ? hx : lx, r.nx() ? lx : hx, r.ny() ? hy : ly, r.ny() ? ly : hy,
+                    r.nz() ? hz : lz, r.nz() ? lz : hz, tentry);
 }
 
 template <bool kCount>
@@ -508,9 +517,9 @@ __device__ __forceinline__ bool visit_node4(const Node4* __restrict__ nodes4, co
   // Planes in node order lo.x, hi.x, lo.y, hi.y, lo.z, hi.z: the near plane
   // of an axis is lo + n (n = 1 for a negative inverse direction).
   const float4* pl = reinterpret_cast<const float4*>(nodes4 + ref);
-  const float4 nx = __ldg(pl + r.nx), fx = __ldg(pl + 1 - r.nx);
-  const float4 ny = __ldg(pl + 2 + r.ny), fy = __ldg(pl + 3 - r.ny);
-  const float4 nz = __ldg(pl + 4 + r.nz), fz = __ldg(pl + 5 - r.nz);
+  const float4 nx = __ldg(pl + r.nx()), fx = __ldg(pl + 1 - r.nx());
+  const float4 ny = __ldg(pl + 2 + r.ny()), fy = __ldg(pl + 3 - r.ny());
+  const float4 nz = __ldg(pl + 4 + r.nz()), fz = __ldg(pl + 5 - r.nz());
   const int4 ch = __ldg(&nodes4[ref].child);
   float t0, t1, t2, t3;
   int r0 = ch.x, r1 = ch.y, r2 = ch.z, r3 = ch.w;
@@ -561,7 +570,7 @@ __device__ __forceinline__ bool test_tri(const Tri* __restrict__ tris,
   load_tri(tris, r, k, X, Y, Z);
   if (kPrecise) {
     const float4* l = tri_lo + 3LL * k;
-    return tri_hit_hl(r, X, Y, Z, __ldg(l + r.kx), __ldg(l + r.ky), __ldg(l + r.kz));
+    return tri_hit_hl(r, X, Y, Z, __ldg(l + r.kx()), __ldg(l + r.ky()), __ldg(l + r.kz()));
   }
   return tri_hit(r, X, Y, Z);
 }
