@@ -91,3 +91,25 @@ def test_bisect_walk_needs_the_persistent_kernel():
     with pytest.raises(ValueError, match="persistent"):
         horizon_svf_comp_py(*d.inputs(), *CASES[2][2], kernel=_lib.HZ_KERNEL_PER_CELL,
                             elev_walk=_lib.HZ_WALK_BISECT)
+
+
+@pytest.mark.parametrize("kernel", [_lib.HZ_KERNEL_PERSISTENT, _lib.HZ_KERNEL_PERSISTENT_BVH2])
+def test_bisect_walk_same_on_both_trees(kernel):
+    """The 4-wide and the binary tree cast the same rays, so the walk gives
+    the same bits on both, in a batch of two domains too."""
+    from horayzon_extpar_gb300.horizon_svf import horizon_svf_comp_batch
+    name, kw, args = CASES[2]
+    d = _domain(kw)
+    h, s = horizon_svf_comp_py(*d.inputs(), *args, elev_walk=_lib.HZ_WALK_BISECT,
+                               kernel=kernel)
+    ho, so, _ = oracle.horizon_svf(*d.inputs(), *args, bisect_walk=True)
+    assert np.mean(np.abs(h - ho) <= EXACT_DEG) >= 0.9999
+    d2 = _domain(CASES[3][1])
+    outs = horizon_svf_comp_batch([(d.inputs(), args), (d2.inputs(), CASES[3][2])],
+                                  elev_walk=_lib.HZ_WALK_BISECT, kernel=kernel)
+    np.testing.assert_array_equal(outs[0][0], h)
+    np.testing.assert_array_equal(outs[0][1], s)
+    h2, s2 = horizon_svf_comp_py(*d2.inputs(), *CASES[3][2], elev_walk=_lib.HZ_WALK_BISECT,
+                                 kernel=kernel)
+    np.testing.assert_array_equal(outs[1][0], h2)
+    np.testing.assert_array_equal(outs[1][1], s2)
