@@ -388,7 +388,8 @@ def learned_small_report(stream, reps=5, parity_cells=20000):
                  {"mlp_azimuth_groups": -1}, "plain_fast_floor": ff,
                  "azimuth_groups_auto_fast_floor": dict(ff, mlp_azimuth_groups=-1),
                  "plain_bisect_walk": dict(BISECT),
-                 "azimuth_groups_auto_bisect_walk": dict(BISECT, mlp_azimuth_groups=-1)}
+                 "azimuth_groups_auto_bisect_walk": dict(BISECT, mlp_azimuth_groups=-1),
+                 "every_azimuth": {"mlp_every_azimuth": True}}
         sample = oracle_sample(d, ARGS, parity_cells) if parity_cells > 0 else None
         for mode, kw in modes.items():
             extra = {} if kw is None else (dict(kw) if mode.startswith("plain") else
@@ -409,6 +410,7 @@ def learned_small_report(stream, reps=5, parity_cells=20000):
             if sample is not None:
                 res[mode]["parity"] = parity_block(h.cpu().numpy(), s.cpu().numpy(), sample)
         for mode, base in (("first_azimuth", "plain"), ("azimuth_groups_auto", "plain"),
+                           ("every_azimuth", "plain"),
                            ("plain_fast_floor", "plain"),
                            ("azimuth_groups_auto_fast_floor", "plain"),
                            ("azimuth_groups_auto_fast_floor", "plain_fast_floor"),
