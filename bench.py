@@ -310,20 +310,23 @@ LEARNED_MODES = {"first_azimuth": dict(),
                  "every_azimuth": dict(mlp_every_azimuth=True),
                  "azimuth_groups_auto": dict(mlp_azimuth_groups=-1),
                  "first_azimuth_fast_floor": dict(elev_floor_deg=FAST_FLOOR_DEG),
-                 "first_azimuth_bisect_walk": dict(BISECT)}
+                 "first_azimuth_bisect_walk": dict(BISECT),
+                 "every_azimuth_bisect_walk": dict(BISECT, mlp_every_azimuth=True)}
 
 
 def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args, sample=None):
     """Learned warm start vs the plain chained search on the headline workload
     (timed like the plain steps: CUDA events around each call). The MLP is
-    trained on 8 other seeds of the same recipe (120 x 120 km boxes).
+    trained on 8 other seeds of the same recipe and domain size (a domain
+    whose cells mostly see past its border would teach the model the void).
     Returns the report and the trained parameters."""
     import torch
 
     from horayzon_extpar_gb300 import horizon_svf_comp_device, synthetic
     params, info = train_mlp(lambda i: synthetic.make_config(
-        "c3", seed=1001 + i, box_km=min(120.0, args.box_km)))
-    info["seeds"] = "8 other seeds, 120 x 120 km boxes of the same recipe"
+        "c3", seed=1001 + i, box_km=args.box_km))
+    info["seeds"] = ("8 other seeds of the same recipe, %g x %g km boxes"
+                     % (args.box_km, args.box_km))
     out = {"training": info}
     evals = dom.ncell * ARGS[0]
     modes = dict(LEARNED_MODES)
@@ -365,7 +368,7 @@ def learned_small_report(stream, reps=5, parity_cells=20000):
     2.5 km / 400 km domain (57k cells; the chain gives one lane per cell and
     its 24 azimuths run one after another) and the 100 m / 150 km domain of
     the learned configuration, each with an MLP trained on 8 other seeds of
-    its own recipe. Per mode: best of `reps` calls (search phase, including
+    its own recipe and size. Per mode: best of `reps` calls (search phase, including
     the learned start's raster, features and MLP, and the whole call on
     device-resident inputs), rays per evaluation, and parity against the
     oracle on a cell sample."""
@@ -373,12 +376,12 @@ def learned_small_report(stream, reps=5, parity_cells=20000):
 
     from horayzon_extpar_gb300 import horizon_svf_comp_device, synthetic
     cases = [("c1", "2.5 km grid, 400x400 km, nhori 24",
-              lambda i: synthetic.make_config("c1", seed=2001 + i, box_km=200.0)),
+              lambda i: synthetic.make_config("c1", seed=2001 + i)),
              ("c4", "100 m grid, 150x150 km, nhori 24",
-              lambda i: synthetic.make_config("c4", seed=3001 + i, box_km=25.0))]
+              lambda i: synthetic.make_config("c4", seed=3001 + i))]
     out = {}
     for key, desc, make_train in cases:
-        params, info = train_mlp(make_train, samples_per_seed=500_000)
+        params, info = train_mlp(make_train)
         d = synthetic.make_config(key, seed=0)
         t = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in d.inputs()]
         evals = d.ncell * ARGS[0]
@@ -389,7 +392,8 @@ def learned_small_report(stream, reps=5, parity_cells=20000):
                  "azimuth_groups_auto_fast_floor": dict(ff, mlp_azimuth_groups=-1),
                  "plain_bisect_walk": dict(BISECT),
                  "azimuth_groups_auto_bisect_walk": dict(BISECT, mlp_azimuth_groups=-1),
-                 "every_azimuth": {"mlp_every_azimuth": True}}
+                 "every_azimuth": {"mlp_every_azimuth": True},
+                 "every_azimuth_bisect_walk": dict(BISECT, mlp_every_azimuth=True)}
         sample = oracle_sample(d, ARGS, parity_cells) if parity_cells > 0 else None
         for mode, kw in modes.items():
             extra = {} if kw is None else (dict(kw) if mode.startswith("plain") else
@@ -411,6 +415,8 @@ def learned_small_report(stream, reps=5, parity_cells=20000):
                 res[mode]["parity"] = parity_block(h.cpu().numpy(), s.cpu().numpy(), sample)
         for mode, base in (("first_azimuth", "plain"), ("azimuth_groups_auto", "plain"),
                            ("every_azimuth", "plain"),
+                           ("every_azimuth_bisect_walk", "plain"),
+                           ("every_azimuth_bisect_walk", "plain_bisect_walk"),
                            ("plain_fast_floor", "plain"),
                            ("azimuth_groups_auto_fast_floor", "plain"),
                            ("azimuth_groups_auto_fast_floor", "plain_fast_floor"),

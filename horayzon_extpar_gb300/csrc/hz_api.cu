@@ -122,7 +122,7 @@ struct Buffers {
   float4* tri_lo;    // precise mode only
   // learned warm start only
   unsigned* rz_bits;
-  float* rz;
+  float4* rz;          // raster quads (RasterDesc::quad)
   long long raster_budget;
   RasterDesc* rdesc;   // device descriptor of the raster
   int16_t* start_m;
@@ -193,7 +193,7 @@ Buffers carve_domain(Carver& c, long long ncell, long long nvert, long long nhor
   if (learned) {
     b.raster_budget = max_mv + max_mv / 10 + 4096;
     b.rz_bits = c.take<unsigned>(b.raster_budget);
-    b.rz = c.take<float>(b.raster_budget);
+    b.rz = c.take<float4>(b.raster_budget);
     b.rdesc = c.take<RasterDesc>(1);
     b.start_m = c.take<int16_t>(L * ncell);
   }

@@ -242,7 +242,10 @@ constexpr int kMlpStartMax = 180;   // +90 deg
 struct RasterDesc {
   float x0, y0, dx, inv_dx;
   int nx, ny;
-  const float* z;  // [ny][nx], -inf where no triangle covers the texel
+  // [ny][nx]: the heights of texel (ix, iy) and of its neighbours (ix + 1,
+  // iy), (ix, iy + 1), (ix + 1, iy + 1), so that a bilinear sample is one
+  // 16-byte load; -inf where no triangle covers a texel.
+  const float4* quad;
 };
 
 struct LearnParams {
@@ -260,9 +263,10 @@ struct LearnParams {
 
 // The height raster of a domain: descriptor (sized from the BVH build's
 // triangle-centre bounds, at most `budget` texels) to *rdesc on the device,
-// then the maximum height of the covering triangles per texel into z.
+// then the maximum height of the covering triangles per texel, as the quads
+// of RasterDesc::quad.
 cudaError_t raster_build(const float* vert32, const int* vot, int n_tri, const unsigned* bounds,
-                         long long budget, RasterDesc* rdesc, unsigned* zbits, float* z,
+                         long long budget, RasterDesc* rdesc, unsigned* zbits, float4* quad,
                          cudaStream_t s);
 // Features of every traced (cell, azimuth); with params (FP32, kMlpParams,
 // device) also the MLP's start index.

@@ -245,7 +245,7 @@ __device__ __forceinline__ void store_row_bf16(__nv_bfloat16* row, const float (
 // texels, as fine as `budget` texels allow. One thread; the descriptor stays
 // on the device, so the learned start needs no host readback.
 __global__ void k_raster_setup(const unsigned* __restrict__ bounds, int n_tri, long long budget,
-                               float* z, RasterDesc* __restrict__ out) {
+                               float4* quad, RasterDesc* __restrict__ out) {
   RasterDesc R;
   R.nx = R.ny = 1;
   R.dx = R.inv_dx = 1.f;
@@ -269,7 +269,7 @@ __global__ void k_raster_setup(const unsigned* __restrict__ bounds, int n_tri, l
     R.x0 = (float)(x0 - 4.0 * dx);
     R.y0 = (float)(y0 - 4.0 * dx);
   }
-  R.z = z;
+  R.quad = quad;
   *out = R;
 }
 
@@ -310,10 +310,23 @@ __global__ void k_raster_tris(const float* __restrict__ vert, const int* __restr
   }
 }
 
-__global__ void k_raster_finish(const unsigned* __restrict__ zi, float* __restrict__ zf,
+__device__ __forceinline__ float raster_texel(const unsigned* __restrict__ zi, long long i) {
+  const unsigned v = __ldg(zi + i);
+  return v == 0u ? -INFINITY : ord2f(v);
+}
+
+// The quads of the finished raster; the last row and column, which no
+// bilinear sample reads, get -inf neighbours.
+__global__ void k_raster_finish(const unsigned* __restrict__ zi, float4* __restrict__ quad,
                                 const RasterDesc* __restrict__ Rp) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < (long long)Rp->nx * Rp->ny) zf[i] = zi[i] == 0u ? -INFINITY : ord2f(zi[i]);
+  const int nx = Rp->nx, ny = Rp->ny;
+  if (i >= (long long)nx * ny) return;
+  const int ix = (int)(i % nx), iy = (int)(i / nx);
+  const bool rx = ix + 1 < nx, ry = iy + 1 < ny;
+  quad[i] = make_float4(raster_texel(zi, i), rx ? raster_texel(zi, i + 1) : -INFINITY,
+                        ry ? raster_texel(zi, i + nx) : -INFINITY,
+                        rx && ry ? raster_texel(zi, i + nx + 1) : -INFINITY);
 }
 
 // Bilinear height; NaN outside the raster or where no triangle covers a corner.
@@ -322,8 +335,8 @@ __device__ __forceinline__ float raster_height(const RasterDesc& R, float x, flo
   const int ix = (int)floorf(fx), iy = (int)floorf(fy);
   if (ix < 0 || iy < 0 || ix + 1 >= R.nx || iy + 1 >= R.ny) return NAN;
   const float ux = fx - ix, uy = fy - iy;
-  const float* z = R.z + (long long)iy * R.nx + ix;
-  const float z00 = __ldg(z), z01 = __ldg(z + 1), z10 = __ldg(z + R.nx), z11 = __ldg(z + R.nx + 1);
+  const float4 c = __ldg(R.quad + (long long)iy * R.nx + ix);
+  const float z00 = c.x, z01 = c.y, z10 = c.z, z11 = c.w;
   if (!(z00 > -INFINITY && z01 > -INFINITY && z10 > -INFINITY && z11 > -INFINITY)) return NAN;
   return (1.f - uy) * ((1.f - ux) * z00 + ux * z01) + uy * ((1.f - ux) * z10 + ux * z11);
 }
@@ -702,13 +715,13 @@ constexpr size_t kTrainSmem = sizeof(MlpWeights) + sizeof(MlpWeightsT) + sizeof(
 }  // namespace
 
 cudaError_t raster_build(const float* vert32, const int* vot, int n_tri, const unsigned* bounds,
-                         long long budget, RasterDesc* rdesc, unsigned* zbits, float* z,
+                         long long budget, RasterDesc* rdesc, unsigned* zbits, float4* quad,
                          cudaStream_t s) {
-  k_raster_setup<<<1, 1, 0, s>>>(bounds, n_tri, budget, z, rdesc);
+  k_raster_setup<<<1, 1, 0, s>>>(bounds, n_tri, budget, quad, rdesc);
   k_raster_fill<<<grid_for(budget, 256), 256, 0, s>>>(zbits, budget);
   if (n_tri > 0)
     k_raster_tris<<<grid_for(n_tri, 128), 128, 0, s>>>(vert32, vot, n_tri, rdesc, zbits);
-  k_raster_finish<<<grid_for(budget, 256), 256, 0, s>>>(zbits, z, rdesc);
+  k_raster_finish<<<grid_for(budget, 256), 256, 0, s>>>(zbits, quad, rdesc);
   note_launches(n_tri > 0 ? 4 : 3);
   return cudaGetLastError();
 }
