@@ -33,11 +33,11 @@ from .horizon_svf import horizon_svf_comp_device
 GRID = {
     "leaf_size": (2, 1, 3, 4, 6),
     "advance_min": (12, 8, 16, 20, 24),
-    "leaf_min": (12, 6, 8, 16, 20),
+    "leaf_min": (1, 2, 4, 8, 12),
     "queue_chunk": (32, 16, 24, 48, 64),
     "kernel": (_lib.HZ_KERNEL_PERSISTENT, _lib.HZ_KERNEL_PERSISTENT_BVH2),
 }
-DEFAULTS = {"leaf_size": 2, "advance_min": 12, "leaf_min": 12, "queue_chunk": 32,
+DEFAULTS = {"leaf_size": 2, "advance_min": 12, "leaf_min": 1, "queue_chunk": 32,
             "kernel": _lib.HZ_KERNEL_PERSISTENT}
 _lock = threading.Lock()
 
