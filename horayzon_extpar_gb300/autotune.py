@@ -32,12 +32,12 @@ from .horizon_svf import horizon_svf_comp_device
 #: Candidate values per knob, in the order the descent visits them.
 GRID = {
     "leaf_size": (2, 1, 3, 4, 6),
-    "advance_min": (12, 8, 16, 20, 24),
+    "advance_min": (16, 12, 20, 8, 24),
     "leaf_min": (1, 2, 4, 8, 12),
     "queue_chunk": (32, 16, 24, 48, 64),
     "kernel": (_lib.HZ_KERNEL_PERSISTENT, _lib.HZ_KERNEL_PERSISTENT_BVH2),
 }
-DEFAULTS = {"leaf_size": 2, "advance_min": 12, "leaf_min": 1, "queue_chunk": 32,
+DEFAULTS = {"leaf_size": 2, "advance_min": 16, "leaf_min": 1, "queue_chunk": 32,
             "kernel": _lib.HZ_KERNEL_PERSISTENT}
 _lock = threading.Lock()
 

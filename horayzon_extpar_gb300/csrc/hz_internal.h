@@ -198,7 +198,7 @@ enum : int {
 // Counter words of the search: 0 rays, 1 node visits, 2 triangle tests; with
 // -DHZ_DIAG, 3.. per-warp loop statistics (printed to stderr by the host).
 constexpr int kCounterWords = 20;
-constexpr int kDefaultAdvanceMin = 12;
+constexpr int kDefaultAdvanceMin = 16;
 // A triangle pass as soon as one lane of the warp holds a postponed leaf:
 // measured fastest on every benchmarked configuration (1.2-2 % against 12).
 constexpr int kDefaultLeafMin = 1;

@@ -375,7 +375,10 @@ constexpr int kFlatBlock = 128;
 #endif
 
 #ifndef HZ_NODE_STEPS
-#define HZ_NODE_STEPS 2  // node visits per lane in one node pass
+#define HZ_NODE_STEPS 3  // node visits per lane in one node pass
+#endif
+#ifndef HZ_TRI_STEPS
+#define HZ_TRI_STEPS 2  // triangle tests per lane in one triangle pass
 #endif
 #ifndef HZ_NODE4_ORDER
 #define HZ_NODE4_ORDER 1  // 0: hit children sorted by entry distance; 1: nearest first only
@@ -1100,17 +1103,23 @@ __global__ void __launch_bounds__(kFlatBlock, HZ_WARP_MIN_BLOCKS)
       }
 #endif
       if ((__popc(pend) >= leaf_min || nodes_left == 0u) && has_leaf) {
-        if (kCount) ntest++;
-        const int k = pl0 >> 4;
-        const bool hit = test_tri<kPrecise>(tris, tri_lo, r, k);
-        pl0 += (1 << 4) - 1;  // next triangle, one fewer left
-        if (hit) {
-          need = true;
-          last_hit = true;
-          si[kOccluder][t] = k;
-        } else if ((pl0 & 15) == 0) {
-          pl0 = 0;  // leaf done: the slot is free again
-          settle();
+        // Up to HZ_TRI_STEPS triangles: the rest of a 2-triangle leaf, or
+        // the first of the next postponed leaf once settle() has moved it up.
+#pragma unroll
+        for (int q = 0; q < HZ_TRI_STEPS; q++) {
+          if (q > 0 && (need || pl0 == 0)) break;
+          if (kCount) ntest++;
+          const int k = pl0 >> 4;
+          const bool hit = test_tri<kPrecise>(tris, tri_lo, r, k);
+          pl0 += (1 << 4) - 1;  // next triangle, one fewer left
+          if (hit) {
+            need = true;
+            last_hit = true;
+            si[kOccluder][t] = k;
+          } else if ((pl0 & 15) == 0) {
+            pl0 = 0;  // leaf done: the slot is free again
+            settle();
+          }
         }
       }
     }
