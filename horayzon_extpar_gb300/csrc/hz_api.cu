@@ -649,9 +649,19 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     // bounds (from the BVH build, on the device), then features + MLP.
     const bool learned = b[0].rz != nullptr;
     long long total = 0, total_items = 0;
+    // Queue order of the domains: least work (cells x azimuths) first, so
+    // that the small domains of a batch complete early (shortest job first:
+    // the lowest mean completion time for the same total work).
+    std::vector<int> queue(n);
+    for (int d = 0; d < n; d++) queue[d] = d;
+    std::stable_sort(queue.begin(), queue.end(), [&](int x, int y) {
+      return (long long)pr[x].cell_count * pr[x].nhori * pr[x].refine <
+             (long long)pr[y].cell_count * pr[y].nhori * pr[y].refine;
+    });
     Fork fk(E, s, n);
     HZ_CUDA(fk.begin());
-    for (int d = 0; d < n; d++) {
+    for (int j = 0; j < n; j++) {
+      const int d = queue[j];
       const Problem& P = pr[d];
       const int L = P.nhori * P.refine;
       HZ_CUDA(trace_tables(b[d].azim_cs, b[d].elev_cs, b[d].svf_lattice, L, shift[d],
@@ -731,7 +741,7 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
       D.L = L;
       D.svf_type = P.svf_type;
       D.tfar = (float)P.dist_search;
-      desc[d] = D;
+      desc[j] = D;  // in queue order: k_begin and item_begin increase with j
       total += P.cell_count;
       total_items += (long long)P.cell_count * P.groups;
     }
