@@ -267,8 +267,9 @@ typedef struct hz_domain {
  * search launch over the cells of all domains. Every domain carries its own
  * arguments (num_hori, grid_type, ...); 1 <= n_domains <= 65535. on_device
  * = 0: host arrays (copied in and out); on_device = 1: device arrays, work
- * enqueued on `stream`. No
- * reference counterpart: the reference computes one domain per call
+ * enqueued on `stream`. The search takes the domains in ascending order of
+ * work (cells x azimuths), so small domains complete first (latency_ms).
+ * No reference counterpart: the reference computes one domain per call
  * (mo_lradtopo_horayzon.cpp:562-785).
  */
 int hz_horizon_svf_batch(hz_domain* domains, int n_domains, int on_device, void* stream,
