@@ -272,6 +272,25 @@ def test_gpu_batch_equals_single_calls():
     assert st["num_rays"] == rays
 
 
+def test_gpu_batch_takes_small_domains_first():
+    """The batch queues its domains by ascending work (cells x azimuths): a
+    large domain given first completes after a small one given last, and
+    every domain still gets its own call's result."""
+    from horayzon_extpar_gb300.horizon_svf import horizon_svf_comp_batch
+    big = synthetic.make_domain(edge_km=1.0, box_km=120.0, seed=41)
+    mid = synthetic.make_domain(edge_km=1.0, box_km=60.0, seed=42)
+    small = synthetic.make_domain(edge_km=1.0, box_km=25.0, seed=43)
+    args = (24, 1, 30000.0, 0.2, 1, 2)
+    doms = [big, mid, small]
+    outs, st = horizon_svf_comp_batch([(d.inputs(), args) for d in doms], return_stats=True)
+    lat = st["latency_ms"]
+    assert lat[2] < lat[0] and lat[1] < lat[0], lat
+    for d, (h, s) in zip(doms, outs):
+        h1, s1 = horizon_svf_comp_py(*d.inputs(), *args)
+        np.testing.assert_array_equal(h, h1)
+        np.testing.assert_array_equal(s, s1)
+
+
 @pytest.mark.parametrize("kernel,leaf_size", [(0, 1), (0, 2), (0, 8), (2, 3), (1, 8)])
 def test_gpu_leaf_size_keeps_results(small_domain, kernel, leaf_size):
     """Triangles per BVH leaf change the tree, not the rays or hit decisions."""
