@@ -274,19 +274,27 @@ def test_gpu_batch_equals_single_calls():
 
 def test_gpu_batch_takes_small_domains_first():
     """The batch queues its domains by ascending work (cells x azimuths): a
-    large domain given first completes after a small one given last, and
-    every domain still gets its own call's result."""
+    domain of more cells than the GPU has resident lanes, given first,
+    completes after a small one given last (whose cells all start in the
+    first wave), and every domain still gets its own call's result."""
     from horayzon_extpar_gb300.horizon_svf import horizon_svf_comp_batch
-    big = synthetic.make_domain(edge_km=1.0, box_km=120.0, seed=41)
-    mid = synthetic.make_domain(edge_km=1.0, box_km=60.0, seed=42)
+    big = synthetic.make_domain(edge_km=1.0, box_km=500.0, seed=41)
     small = synthetic.make_domain(edge_km=1.0, box_km=25.0, seed=43)
-    args = (24, 1, 30000.0, 0.2, 1, 2)
-    doms = [big, mid, small]
-    outs, st = horizon_svf_comp_batch([(d.inputs(), args) for d in doms], return_stats=True)
+    assert big.ncell > 250_000
+    # A domain completes with its slowest cell, and a cell at a border that
+    # looks out over the void walks down towards -85 deg and, at its next
+    # azimuth, back up, one ray per step: the early floor (-0.25 deg) ends
+    # those walks at the clip. 4 azimuths: a small-domain cell is a few rays
+    # (a cell of 24 azimuths takes several ms of a loaded GPU, a good part of
+    # the big domain's 3.5 waves of cells).
+    calls = [(big, (24, 1, 30000.0, 0.2, 1, 2)), (small, (4, 1, 3000.0, 0.2, 1, 2))]
+    floor = -0.25
+    outs, st = horizon_svf_comp_batch([(d.inputs(), a) for d, a in calls], return_stats=True,
+                                      elev_floor_deg=floor)
     lat = st["latency_ms"]
-    assert lat[2] < lat[0] and lat[1] < lat[0], lat
-    for d, (h, s) in zip(doms, outs):
-        h1, s1 = horizon_svf_comp_py(*d.inputs(), *args)
+    assert lat[1] < 0.5 * lat[0], lat
+    for (d, args), (h, s) in zip(calls, outs):
+        h1, s1 = horizon_svf_comp_py(*d.inputs(), *args, elev_floor_deg=floor)
         np.testing.assert_array_equal(h, h1)
         np.testing.assert_array_equal(s, s1)
 
