@@ -458,6 +458,20 @@ struct RunOut {
   std::vector<double> origin_lat, origin_lon;  // ENU origin per domain [deg]
 };
 
+// Resident threads of the current device (SMs x min(threads per SM, 1024)).
+int resident_lanes(long long* lanes) {
+  int dev = 0, sms = 0, threads = 0;
+  HZ_CUDA(cudaGetDevice(&dev));
+  HZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  HZ_CUDA(cudaDeviceGetAttribute(&threads, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
+  *lanes = (long long)sms * std::min(threads, 1024);
+  return HZ_OK;
+}
+
+// Searches of more items than this many times the resident lanes queue the
+// border cells of each domain first (run_batch).
+constexpr long long kBorderFirstWaves = 4;
+
 // Runs the pipeline for n domains whose arrays are device pointers in pr[].
 // With stop != kFull it ends after the mesh (or ENU) stage and leaves the
 // results in b[].
@@ -649,6 +663,16 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
     // bounds (from the BVH build, on the device), then features + MLP.
     const bool learned = b[0].rz != nullptr;
     long long total = 0, total_items = 0;
+    // Border cells (of a vertex with a -2 entry) search several times as long
+    // as inner ones; when the call's items fill the GPU's lanes several times
+    // over they are queued first in each domain, so that none starts in the
+    // search's last wave. In a single wave the Hilbert order, which spreads
+    // them over the warps of the border's neighbourhood, is faster.
+    long long items = 0, lanes = 0;
+    for (int d = 0; d < n; d++) items += (long long)pr[d].cell_count * pr[d].groups;
+    const int rl = resident_lanes(&lanes);
+    if (rl) return rl;
+    const bool border_first = items >= kBorderFirstWaves * lanes;
     // Queue order of the domains: least work (cells x azimuths) first, so
     // that the small domains of a batch complete early (shortest job first:
     // the lowest mean completion time for the same total work).
@@ -697,7 +721,9 @@ int run_batch(Engine& E, const Problem* pr, const Buffers* b, int n, const Batch
         q.start_m = b[d].start_m;
         HZ_CUDA(learn_features(q, opt.mlp_params ? bb.mlp : nullptr, fk.on(d)));
       }
-      HZ_CUDA(cell_order(b[d].cell_enu, P.cell_begin, P.cell_count, (int)(total - P.cell_begin),
+      HZ_CUDA(cell_order(b[d].cell_enu, border_first ? P.cov : nullptr, P.nvert, P.ncell,
+                         P.cell_begin, P.cell_count,
+                         (int)(total - P.cell_begin),
                          bb.order + total, b[d].order_scratch, b[d].cell_bounds, bb.work,
                          fk.on(d)));
       DomainDesc D;
@@ -941,11 +967,10 @@ int azimuth_groups(const hz_domain* doms, int n, const hz_options& opt, int* gro
     return HZ_OK;
   }
   if (G != -1) return fail(HZ_ERR_VALUE, "mlp_azimuth_groups must be -1, 0 or >= 1");
-  int dev = 0, sms = 0, threads = 0;
-  HZ_CUDA(cudaGetDevice(&dev));
-  HZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  HZ_CUDA(cudaDeviceGetAttribute(&threads, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
-  const long long target = (long long)kItemsPerLane * sms * std::min(threads, 1024);
+  long long lanes = 0;
+  const int rc = resident_lanes(&lanes);
+  if (rc) return rc;
+  const long long target = (long long)kItemsPerLane * lanes;
   long long cells = 0;
   for (int d = 0; d < n; d++)
     cells += opt.cell_count > 0 && n == 1 ? opt.cell_count : doms[d].num_cell;

@@ -131,9 +131,11 @@ cudaError_t trace_exact(const TraceParams& p, bool count_work, cudaStream_t s);
 // the work counter used by trace_flat.
 // Work ids are id_offset + cell.
 size_t cell_order_scratch_bytes(long long n);
-cudaError_t cell_order(const double* cell_enu, int begin, int count, int id_offset,
-                       int32_t* order, void* scratch, unsigned* bounds, int* work,
-                       cudaStream_t s);
+// With cov (device cells_of_vertex, nv vertices, ncell cells of the domain)
+// the cells of border vertices come first.
+cudaError_t cell_order(const double* cell_enu, const int* cov, int nv, int ncell, int begin,
+                       int count, int id_offset, int32_t* order, void* scratch,
+                       unsigned* bounds, int* work, cudaStream_t s);
 
 // One domain of the persistent search (device-resident array).
 struct DomainDesc {

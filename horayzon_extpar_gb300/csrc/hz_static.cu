@@ -288,7 +288,8 @@ extern "C" int hz_horizon_svf_device_static(
   // Pageable source: the copy has finished with `D` when the call returns.
   HZ_STATIC_CUDA(cudaMemcpyAsync(b.dom, &D, sizeof(D), cudaMemcpyHostToDevice, s),
                  "search descriptor");
-  HZ_STATIC_CUDA(cell_order(b.cell_enu, 0, num_cell, 0, b.order, b.order_scratch, b.cell_bounds,
+  HZ_STATIC_CUDA(cell_order(b.cell_enu, nullptr, 0, num_cell, 0, num_cell, 0, b.order,
+                            b.order_scratch, b.cell_bounds,
                             b.work, s), "cell order");
   HZ_STATIC_CUDA(trace_tables(b.azim_cs, b.elev_cs, b.svf_lattice, L, azim_shift, D.hori_acc,
                               D.svf_type, s), "lattice tables");

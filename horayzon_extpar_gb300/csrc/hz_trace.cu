@@ -1336,8 +1336,31 @@ __device__ __forceinline__ uint32_t hilbert16(uint32_t x, uint32_t y) {
   return d;
 }
 
+// Cells of a border vertex (a vertex with a -2 entry in cells_of_vertex, the
+// reference's border, functions.py:58-97): the edge row, whose searches look
+// out over the void and cost several times an inner cell's.
+__global__ void k_mark_border(const int* __restrict__ cov, int nv, int ncell,
+                              uint8_t* __restrict__ border) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  bool edge = false;
+#pragma unroll
+  for (int j = 0; j < 6; j++) edge |= cov[(long long)nv * j + v] == -2;
+  if (!edge) return;
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    const int c = cov[(long long)nv * j + v];
+    if (c >= 0 && c < ncell) border[c] = 1;
+  }
+}
+
+// Queue key of a cell: its Hilbert index (or Morton) shifted right by one,
+// with the top bit set for cells off the border, so that the border cells,
+// the longest searches, are queued first (longest job first: the search's
+// last wave then holds no border cell).
 __global__ void k_cell_keys(const double* __restrict__ cell_enu, int begin, int count,
                             int id_offset, const unsigned* __restrict__ bounds,
+                            const uint8_t* __restrict__ border,
                             uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
@@ -1350,10 +1373,12 @@ __global__ void k_cell_keys(const double* __restrict__ cell_enu, int begin, int 
   const uint32_t qx = fx <= 0.f ? 0u : (fx >= 65535.0f ? 65535u : (uint32_t)fx);
   const uint32_t qy = fy <= 0.f ? 0u : (fy >= 65535.0f ? 65535u : (uint32_t)fy);
 #if HZ_CELL_ORDER == 1
-  keys[k] = hilbert16(qx, qy);
+  const uint32_t key = hilbert16(qx, qy);
 #else
-  keys[k] = spread16(qx) | (spread16(qy) << 1);
+  const uint32_t key = spread16(qx) | (spread16(qy) << 1);
 #endif
+  const bool first = border != nullptr && border[begin + k] != 0;
+  keys[k] = (key >> 1) | (first ? 0u : 0x80000000u);
   vals[k] = id_offset + begin + k;
 }
 
@@ -1396,12 +1421,12 @@ cudaError_t trace_tables(double2* azim_cs, double2* elev_cs, double* svf_lattice
 
 size_t cell_order_scratch_bytes(long long n) {
   if (n < 1) n = 1;
-  return 4 * sizeof(uint32_t) * (size_t)n + radix_scratch_u32(n) + 64 + 5 * 256;
+  return 4 * sizeof(uint32_t) * (size_t)n + (size_t)n + radix_scratch_u32(n) + 64 + 6 * 256;
 }
 
-cudaError_t cell_order(const double* cell_enu, int begin, int count, int id_offset,
-                       int32_t* order, void* scratch, unsigned* bounds, int* work,
-                       cudaStream_t s) {
+cudaError_t cell_order(const double* cell_enu, const int* cov, int nv, int ncell, int begin,
+                       int count, int id_offset, int32_t* order, void* scratch,
+                       unsigned* bounds, int* work, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
   char* base = (char*)scratch;
   auto take = [&](size_t bytes) {
@@ -1413,10 +1438,18 @@ cudaError_t cell_order(const double* cell_enu, int begin, int count, int id_offs
   uint32_t* keys_alt = (uint32_t*)take(sizeof(uint32_t) * count);
   int32_t* vals_alt = (int32_t*)take(sizeof(int32_t) * count);
   void* sort_scratch = take(radix_scratch_u32(count));
+  uint8_t* border = nullptr;
+  if (cov != nullptr && nv > 0 && ncell > 0) {
+    border = (uint8_t*)take((size_t)ncell);
+    cudaError_t e = cudaMemsetAsync(border, 0, (size_t)ncell, s);
+    if (e != cudaSuccess) return e;
+    k_mark_border<<<grid_for(nv, 256), 256, 0, s>>>(cov, nv, ncell, border);
+    note_launches(1);
+  }
   k_init_cell_bounds<<<1, 1, 0, s>>>(bounds, work);
   k_cell_bounds<<<grid_for(count, 256), 256, 0, s>>>(cell_enu, begin, count, bounds);
   k_cell_keys<<<grid_for(count, 256), 256, 0, s>>>(cell_enu, begin, count, id_offset, bounds,
-                                                   keys, order);
+                                                   border, keys, order);
   note_launches(3);
   return radix_sort_pairs(keys, order, keys_alt, vals_alt, count, 32, sort_scratch, s);
 }
