@@ -360,7 +360,44 @@ def learned_report(dom, d_in, h_ref, s_ref, stream, plain_ms, args, sample=None)
             out[mode]["groups"] = auto_groups(dom.ncell, ARGS[0])
         if sample is not None:
             out[mode]["parity"] = parity_block(h.cpu().numpy(), s.cpu().numpy(), sample)
+    out["perfect_start_ceiling"] = perfect_start_ceiling(d_in, dom.ncell, stream, plain_ms,
+                                                         args)
     return out, params
+
+
+def perfect_start_ceiling(d_in, ncell, stream, plain_ms, args):
+    """The learned start's measured ceiling on this workload: every azimuth
+    restarted at the start a perfect model would propose, the lattice index
+    of the plain search's own result ((j + 1) / 2 for the unclipped horizon
+    j * 0.25 deg, which casts two rays where visibility is monotone), given
+    as start indices (no model cost). Timed like the learned modes."""
+    import torch
+
+    from horayzon_extpar_gb300 import horizon_svf_comp_device
+    L = ARGS[0] * ARGS[4]
+    raw = torch.empty((L, ncell), dtype=torch.int16, device=d_in[0].device)
+    horizon_svf_comp_device(*d_in, *ARGS, stream=stream, raw_index=raw)
+    start = torch.clamp(torch.div(raw.to(torch.int32) + 1, 2, rounding_mode="floor"),
+                        -170, 180).to(torch.int16).contiguous()
+    out = {"what": "every azimuth started at the plain search's own result (a perfect "
+                   "proposal, no model cost); the bound on any learned start here"}
+    for name, kw in (("reference_walk", {}), ("bisect_walk", dict(BISECT))):
+        kw = dict(kw, start_index=start, mlp_every_azimuth=True)
+        for _ in range(max(1, args.warmup)):
+            horizon_svf_comp_device(*d_in, *ARGS, stream=stream, **kw)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        rays = 0
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            _, _, st = horizon_svf_comp_device(*d_in, *ARGS, stream=stream, **kw)
+            ev[k][1].record(stream)
+            rays = st["num_rays"]
+        torch.cuda.synchronize()
+        ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+        out[name] = {"ms_per_step": ms, "speedup_vs_plain": plain_ms / ms,
+                     "rays_per_eval": rays / (ncell * ARGS[0])}
+    return out
 
 
 def learned_small_report(stream, reps=5, parity_cells=20000):
