@@ -28,6 +28,45 @@ def test_header_declares_expected_entry_points():
     assert set(names) == set(_lib.EXPORTED_SYMBOLS), names
 
 
+def _struct_fields(name):
+    """Member names of `typedef struct { ... } name;` in the public header."""
+    src = open(os.path.join(ROOT, "include", "horayzon_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    end = src.index("} %s;" % name)
+    body = src[src.rindex("typedef struct", 0, end):end]
+    body = body[body.index("{") + 1:]
+    names = []
+    for decl in body.split(";"):
+        parts = [re.sub(r"\[[^\]]*\]", "", p).strip() for p in decl.split(",")]
+        if not parts[0]:
+            continue
+        names += [re.findall(r"\w+", p)[-1] for p in parts]
+    return names
+
+
+def test_python_structs_mirror_the_header():
+    """ctypes mirrors of hz_options, hz_stats and hz_domain: the same members
+    in the same order as the header."""
+    import ctypes as C
+    for cls, name in ((_lib.Options, "hz_options"), (_lib.Stats, "hz_stats"),
+                      (_lib.Domain, "hz_domain")):
+        assert [f for f, _ in cls._fields_] == _struct_fields(name), name
+    assert C.sizeof(_lib.Options) > 0
+
+
+def test_default_options_from_the_library():
+    """hz_default_options (no GPU needed) fills the struct the Python layer
+    passes: its size field is the ctypes struct's size, and the documented
+    defaults hold."""
+    import ctypes as C
+    o = _lib.Options()
+    _lib.load().hz_default_options(C.byref(o))
+    assert o.size == C.sizeof(_lib.Options)
+    assert o.device == -1 and o.elev_floor_deg == -85.0
+    assert o.occluder_cache == 1 and o.elev_walk == _lib.HZ_WALK_REFERENCE
+    assert o.advance_min == 0 and o.leaf_min == 0  # 0: the library's defaults
+
+
 def test_library_exports_every_declared_symbol():
     L = _lib.load()
     for name in declared_functions():
